@@ -1,0 +1,345 @@
+"""Throughput benchmark of the GB300 coarsening path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload rmat22]
+
+One step = one full multilevel coarsening (cuMetis_coarsen's loop: matching,
+coarse map, contraction per level, reference stop rule) of the workload.
+Metric: coarsened edges/s = sum over levels of the level's directed entries m,
+divided by the time.  `value` is measured with the input resident in HBM;
+`e2e` goes through the public C-ABI call with pinned host buffers: host->device
+copy of the input, coarsening, device->host copy of the coarsest graph.
+
+--impl reference times the reference's CPU coarsening (cuMetis_cpu_match +
+cuMetis_cpu_create_cgraph, cuMetis.cu:737-918, as restated in the oracle; the
+reference tree is not available where the benchmark runs) on the same
+workload, same metric.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+
+WORKLOADS = {
+    # name: (generator, nparts, description)
+    "rmat22": (lambda cm: cm.gen_rmat(22, 16, 0.57, 0.19, 0.19, 1, 1, 100), 256,
+               "R-MAT scale 22, edge factor 16, (a,b,c,d)=(.57,.19,.19,.05), weights U[1,100], k=256"),
+    "grid725": (lambda cm: cm.gen_grid2d(725, 725), 64, "2D 5-point grid 725x725, unit weights, k=64"),
+    "tri69": (lambda cm: cm.gen_tri_grid(69, 69), 8, "2D triangulated grid 69x69, unit weights, k=8"),
+}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def level_bytes(sizes):
+    """Algorithmic HBM bytes of each coarsening level (int32 arrays, each
+    touched once): matching 4(2m+3n+1), coarse map 4(2n), contraction
+    4(3m+3n+1) + 4(2m'+2n'+1)."""
+    out = []
+    for (n, m), (cn, cm_) in zip(sizes[:-1], sizes[1:]):
+        out.append(4 * (5 * m + 2 * cm_ + 8 * n + 2 * cn + 3))
+    return out
+
+
+def dist_setup(n_gpus):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if os.environ.get("CM_BENCH_BACKEND") != "gloo" else "gloo")
+    return ws, rank, local
+
+
+def allreduce_max(x, ws, device):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def run_reference(args, ws, rank):
+    """CPU baseline arm: the reference's CPU coarsening (restated) on the host."""
+    if rank != 0:
+        return
+    import cumetis_gb300 as cm
+    from oracle import oracle as O
+    gen, k, desc = WORKLOADS[args.workload]
+    g = gen(cm)
+    og = O.CSR(g.xadj, g.adjncy, g.adjwgt, g.vwgt)
+    thr = cm.coarsen_threshold(g.nvtxs, k)
+    mv = O.maxvwgt_rule(int(g.vwgt.sum()), thr)
+
+    def step():
+        O.srand(1)
+        cur, units = og, 0
+        while True:
+            cg, _, _ = O.ref_cpu_coarsen_level(cur, mv)
+            units += cur.m
+            prev, cur = cur, cg
+            if not (cur.n > thr and cur.n < 0.75 * prev.n and cur.m > cur.n // 2):
+                break
+        return units
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    units = 0
+    for _ in range(args.steps):
+        units += step()
+    dt = time.perf_counter() - t0
+    v = units / dt
+    line = {"metric": "coarsened edges/s", "value": v, "unit": "edges/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": args.workload, "description": desc, "nvtxs": g.nvtxs, "nedges": g.nedges,
+                       "nparts": k, "coarsen_threshold": thr, "maxvwgt": mv},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "edges/s", "cores": 1, "kind": "port",
+                             "sample": "full multilevel coarsening of the workload per step (reference CPU "
+                                       "matching + contraction, single-threaded as in the reference)"},
+            "e2e": {"value": v, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(g, k, budget_s=20.0):
+    from oracle import oracle as O
+    import cumetis_gb300 as cm
+    og = O.CSR(g.xadj, g.adjncy, g.adjwgt, g.vwgt)
+    thr = cm.coarsen_threshold(g.nvtxs, k)
+    mv = O.maxvwgt_rule(int(g.vwgt.sum()), thr)
+    O.srand(1)
+    t0 = time.perf_counter()
+    units, reps = 0, 0
+    while time.perf_counter() - t0 < budget_s or reps == 0:
+        cg, _, _ = O.ref_cpu_coarsen_level(og, mv)
+        units += og.m
+        reps += 1
+    dt = time.perf_counter() - t0
+    return {"value": units / dt, "unit": "edges/s", "cores": 1, "kind": "port",
+            "sample": "%d x level 0 of the workload (reference CPU matching + contraction, restated; %.1f s)" %
+                      (reps, dt)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="rmat22", choices=sorted(WORKLOADS))
+    ap.add_argument("--mode", type=int, default=0, help="matching mode (0 = heaviest edge, ties to lower id)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    ws, rank, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        barrier(ws)
+        return
+
+    import torch
+    import cumetis_gb300 as cm
+    torch.cuda.set_device(local)
+    dev = "cuda:%d" % local
+    gen, k, desc = WORKLOADS[args.workload]
+    g = gen(cm)
+    thr = cm.coarsen_threshold(g.nvtxs, k)
+    ctx = cm.Context(local)
+    ctx.reserve(g.nvtxs, g.nedges)
+    dg = g.to_device(dev)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        h = ctx.coarsen(dg, thr, args.mode)
+        sizes = h.sizes()
+        h.close()
+        return sizes
+
+    for _ in range(args.warmup):
+        sizes = step()
+    units_per_step = sum(m for (_, m) in sizes[:-1])
+
+    # ---- device-resident timed region ------------------------------------
+    ctx.set_stage_timing(True)
+    ctx.stage_times(reset=True)
+    launches0 = ctx.launch_count()
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(ws)
+    launches = ctx.launch_count() - launches0
+    stages = ctx.stage_times(reset=True)
+    ctx.set_stage_timing(False)
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = allreduce_max(ms, ws, dev)
+    value = units_per_step * ws / (ms / 1e3)
+
+    # ---- roofline of the dominant kernel -----------------------------------
+    peak, peak_kind = measured_peaks()
+    lb = level_bytes(sizes)
+    n0, m0 = sizes[0]
+    stage_bytes = {
+        # per launch, summed over levels
+        "k_match": sum(4 * (2 * m + 3 * n + 1) for (n, m) in sizes[:-1]),
+        "k_contract_tiles": sum(4 * (3 * m + 3 * n + 1) + 4 * (2 * cm_ + 2 * cn + 1)
+                                for (n, m), (cn, cm_) in zip(sizes[:-1], sizes[1:])),
+    }
+    dom = max(stages, key=lambda k_: stages[k_]) if stages else None
+    per_step_ms = {k_: v / args.steps for k_, v in stages.items()}
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            tj = json.load(f).get(args.workload, {})
+        traffic = tj.get(dom)
+    except Exception:
+        pass
+    roof = None
+    if dom is not None and dom in stage_bytes and per_step_ms[dom] > 0:
+        ach = stage_bytes[dom] / (per_step_ms[dom] / 1e3) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "peak_kind": peak_kind, "traffic": traffic}
+    level_ach = sum(lb) / (ms / 1e3) / 1e9
+
+    # ---- end to end through the C ABI with pinned host buffers --------------
+    pin = {a: torch.empty(getattr(g, a).shape[0], dtype=torch.int32, pin_memory=True) for a in
+           ("xadj", "adjncy", "adjwgt", "vwgt")}
+    for a, t in pin.items():
+        t.numpy()[:] = getattr(g, a)
+    hg = cm.Graph(*(pin[a].numpy() for a in ("xadj", "adjncy", "adjwgt", "vwgt")))
+    cn_, cm2 = sizes[-1]
+    out = {a: torch.empty(max(s, 1), dtype=torch.int32, pin_memory=True)
+           for a, s in (("xadj", cn_ + 1), ("adjncy", cm2), ("adjwgt", cm2), ("vwgt", cn_))}
+
+    def e2e_step():
+        h = ctx.coarsen(hg, thr, args.mode)
+        last = len(h) - 1
+        h.read_level(last, out["xadj"].data_ptr(), out["adjncy"].data_ptr(), out["adjwgt"].data_ptr(),
+                     out["vwgt"].data_ptr())
+        h.close()
+
+    for _ in range(2):
+        e2e_step()
+    barrier(ws)
+    torch.cuda.synchronize()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e2.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e3.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max(e2.elapsed_time(e3), (time.perf_counter() - t0) * 1e3) / args.steps
+    e2e_ms = allreduce_max(e2e_ms, ws, dev)
+    h2d = 4 * (2 * n0 + 1 + 2 * m0)
+    d2h = 4 * (2 * cn_ + 1 + 2 * cm2)
+
+    line = {"metric": "coarsened edges/s", "value": value, "unit": "edges/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": args.workload, "description": desc, "nvtxs": n0, "nedges": m0, "nparts": k,
+                       "coarsen_threshold": thr, "levels": [list(s) for s in sizes], "match_mode": args.mode,
+                       "parallelism": "replicas" if ws > 1 else "single-gpu",
+                       "l2": "inputs larger than L2 (%.0f MB of CSR)" % (4 * (2 * n0 + 2 * m0) / 1e6),
+                       "level_roofline_frac": level_ach / peak, "level_achieved_gbs": level_ach,
+                       "stage_ms_per_step": per_step_ms},
+            "roofline": roof, "clocks": clk, "gpu_launches": launches,
+            "e2e": {"value": units_per_step * ws / (e2e_ms / 1e3), "unit": "edges/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms}}
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(g, k)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    barrier(ws)
+
+
+if __name__ == "__main__":
+    main()

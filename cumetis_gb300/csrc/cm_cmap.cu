@@ -1,0 +1,162 @@
+// cm_cmap.cu -- coarse-vertex map in one pass with a decoupled look-back scan.
+//
+// Replaces (cuMetis.cu) findc1/findc2 (1621-1646), thrust::inclusive_scan over
+// the leader flags (1758), findc2_5 + the blocking D2H of cnvtxs (1651, 1770),
+// findc3/findc4 (1660-1694), the D2H of the degree bounds (1789) and the host
+// thrust::exclusive_scan + H2D of the expanded row offsets (1304-1309).
+//
+// One tile = 2048 fine vertices (8 warps x 8 steps x 32 lanes, coalesced).
+// Each vertex contributes the packed pair (leader ? 1 : 0, leader ? L : 0),
+// L = deg(v) + deg(match[v]) the expanded coarse-row length, as
+// (count << 31 | L); one 64-bit look-back scan yields both the coarse id and
+// the expanded offset of every leader.  HBM traffic per vertex: match (4 B),
+// xadj (4 B), vwgt (4 B) read; cmap (4 B) written; leader/cvwgt/eoff
+// (12 B per coarse vertex) written.
+#include "cm_ctx.h"
+
+namespace cm {
+namespace {
+
+constexpr int kCmapThreads = 256;
+constexpr int kCmapSteps = 8;
+constexpr int kCmapTile = kCmapThreads * kCmapSteps;  // 2048 vertices
+constexpr unsigned long long kMask31 = (1ull << 31) - 1;
+
+__global__ void __launch_bounds__(kCmapThreads)
+k_cmap(int n, const int *__restrict__ xadj, const int *__restrict__ vwgt, const int *__restrict__ match,
+       int *__restrict__ cmap, int *__restrict__ leader, int *__restrict__ cvwgt, int *__restrict__ eoff,
+       int *__restrict__ d_cnvtxs, int *__restrict__ long_list, int long_thr, unsigned long long *long_ctr,
+       int long_chunk, int *__restrict__ chunk_row, int *__restrict__ first_row, int tile_diag,
+       unsigned long long *__restrict__ lb, DevStatus *st) {
+  __shared__ int s_tile;
+  __shared__ unsigned long long s_warp[kCmapThreads / 32];
+  __shared__ unsigned long long s_excl;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd((unsigned long long *)lb, 1ull);
+  __syncthreads();
+  const int tile = s_tile;
+  const long long wbase = (long long)tile * kCmapTile + wid * (32 * kCmapSteps);
+
+  unsigned long long pre[kCmapSteps];
+  unsigned long long carry = 0;
+#pragma unroll
+  for (int it = 0; it < kCmapSteps; ++it) {
+    const long long v = wbase + it * 32 + lane;
+    unsigned long long val = 0;
+    if (v < n) {
+      int u = match[v];
+      if (u < 0 || u >= n) {  // not a matching: treat as singleton, report
+        record_error(st, CM_ERR_INVALID, ERR_SITE_MATCH_INVALID);
+        u = (int)v;
+      }
+      if (v <= u) {
+        int L = xadj[v + 1] - xadj[v];
+        if (u != v) L += xadj[u + 1] - xadj[u];
+        val = (1ull << 31) | (unsigned long long)L;
+      }
+    }
+    unsigned long long x = warp_inclusive_scan_u64(val);
+    pre[it] = carry + x - val;  // exclusive within the warp slice
+    carry += __shfl_sync(0xffffffffu, x, 31);
+  }
+  if (lane == 0) s_warp[wid] = carry;
+  __syncthreads();
+  if (wid == 0) {
+    unsigned long long w = lane < kCmapThreads / 32 ? s_warp[lane] : 0ull;
+    unsigned long long wi = warp_inclusive_scan_u64(w);
+    unsigned long long agg = __shfl_sync(0xffffffffu, wi, kCmapThreads / 32 - 1);
+    if (lane < kCmapThreads / 32) s_warp[lane] = wi - w;
+    unsigned long long ex = lookback_exclusive(lb, tile, agg, st);
+    if (lane == 0) s_excl = ex;
+  }
+  __syncthreads();
+  const unsigned long long tbase = s_excl + s_warp[wid];
+  int row_max = 0;
+#pragma unroll
+  for (int it = 0; it < kCmapSteps; ++it) {
+    const long long v = wbase + it * 32 + lane;
+    if (v >= n) continue;
+    int u = match[v];
+    if (u < 0 || u >= n) u = (int)v;
+    const unsigned long long P = tbase + pre[it];
+    if (v <= u) {
+      const int c = (int)(P >> 31);
+      const int e = (int)(P & kMask31);
+      const int L = (xadj[v + 1] - xadj[v]) + (u != v ? xadj[u + 1] - xadj[u] : 0);
+      cmap[v] = c;
+      leader[c] = (int)v;
+      cvwgt[c] = (int)((unsigned)vwgt[v] + (u != v ? (unsigned)vwgt[u] : 0u));
+      eoff[c] = e;
+      if (first_row) {
+        // Contraction tiles cover diagonals [kD, (k+1)D) of (row + entry)
+        // space; tile k starts at the first row whose diagonal c+eoff[c] >= kD.
+        const long long d0 = (long long)c + e, d1 = d0 + 1 + L;
+        for (long long k = d0 / tile_diag + 1; k <= d1 / tile_diag; ++k) first_row[k] = c + 1;
+        if (c == 0) first_row[0] = 0;
+      }
+      if (L > long_thr) {
+        const int nch = (L + long_chunk - 1) / long_chunk;
+        unsigned long long old = atomicAdd(long_ctr, (1ull << 32) | (unsigned long long)nch);
+        const int idx = (int)(old >> 32);
+        const int cbase = (int)(old & 0xffffffffu);
+        long_list[2 * idx] = c;
+        long_list[2 * idx + 1] = cbase;  // first chunk index of this row
+        for (int j = 0; j < nch; ++j) chunk_row[cbase + j] = idx;
+      }
+      row_max = L > row_max ? L : row_max;
+    }
+    if (v == n - 1) {  // the last vertex closes the scan
+      const unsigned long long inc = P + ((v <= u) ? ((1ull << 31) | (unsigned long long)((xadj[v + 1] - xadj[v]) +
+                                                                                      (u != v ? xadj[u + 1] - xadj[u] : 0)))
+                                                   : 0ull);
+      const int cn = (int)(inc >> 31);
+      *d_cnvtxs = cn;
+      eoff[cn] = (int)(inc & kMask31);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) row_max = max(row_max, __shfl_xor_sync(0xffffffffu, row_max, o));
+  if (lane == 0 && row_max > 0) atomicMax(&st->max_row, row_max);
+}
+
+// Followers take their leader's id; also checks that match is an involution.
+__global__ void k_cmap_followers(int n, const int *__restrict__ match, int *__restrict__ cmap, DevStatus *st) {
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+    int u = match[v];
+    if (u < 0 || u >= n) continue;  // already reported by k_cmap
+    if (u != v && match[u] != v) record_error(st, CM_ERR_INVALID, ERR_SITE_MATCH_INVALID);
+    if (u < v) cmap[v] = cmap[u];
+  }
+}
+
+}  // namespace
+
+size_t cmap_ws_bytes(int64_t n) { return (size_t)((n + kCmapTile - 1) / kCmapTile + 2) * 8 + 256; }
+
+int launch_cmap(cm_ctx *ctx, int32_t n, const int32_t *xadj, const int32_t *vwgt, const int32_t *match,
+                int32_t *cmap, int32_t *leader, int32_t *cvwgt, int32_t *eoff, int32_t *d_cnvtxs,
+                int32_t *long_list, int32_t long_threshold, int32_t long_chunk, unsigned long long *d_long_ctr,
+                int32_t *chunk_row, int32_t *first_row, int32_t tile_diag, cudaStream_t s) {
+  if (n == 0) {
+    cudaMemsetAsync(d_cnvtxs, 0, sizeof(int32_t), s);
+    cudaMemsetAsync(eoff, 0, sizeof(int32_t), s);
+    return cuda_status(cudaGetLastError(), "cmap(empty)");
+  }
+  const int ntiles = (n + kCmapTile - 1) / kCmapTile;
+  unsigned long long *lb = (unsigned long long *)ws_take(ctx, (size_t)(ntiles + 1) * 8);
+  if (!lb) return cm_fail(CM_ERR_NOMEM, "cmap: workspace too small");
+  cudaMemsetAsync(lb, 0, (size_t)(ntiles + 1) * 8, s);
+  stage_begin(ctx, s);
+  k_cmap<<<ntiles, kCmapThreads, 0, s>>>(n, xadj, vwgt, match, cmap, leader, cvwgt, eoff, d_cnvtxs, long_list,
+                                          long_list ? long_threshold : INT32_MAX, d_long_ctr,
+                                          long_chunk > 0 ? long_chunk : 1, chunk_row, first_row,
+                                          tile_diag > 0 ? tile_diag : 1, lb, ctx->d_status);
+  ctx->launches++;
+  int blocks = ctx->num_sms * 8;
+  k_cmap_followers<<<blocks, 256, 0, s>>>(n, match, cmap, ctx->d_status);
+  stage_end(ctx, CM_STAGE_CMAP, s);
+  ctx->launches++;
+  return check_launch(ctx, "cmap");
+}
+
+}  // namespace cm

@@ -1,0 +1,65 @@
+// cm_ctx.h -- the device context behind the opaque cm_ctx handle (internal).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+#include "cm_device.cuh"
+
+struct cm_ctx {
+  int device = 0;
+  int num_sms = 0;
+  int max_smem_optin = 0;       // bytes of dynamic shared memory a block may opt into
+  cm::DevStatus *d_status = nullptr;   // device status block
+  cm::DevStatus *h_status = nullptr;   // pinned host mirror for readbacks
+  int32_t *h_small = nullptr;          // pinned 64-byte readback buffer
+  char *ws = nullptr;           // device workspace (grown on demand)
+  size_t ws_bytes = 0;
+  size_t ws_used = 0;           // bump pointer of the current call
+  int64_t launches = 0;         // kernels launched by this context
+  // stage timing (CUDA events around kernels)
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  struct Pending { int stage; cudaEvent_t a, b; };
+  std::vector<Pending> pending;
+  double stage_ms[CM_STAGE_COUNT] = {0};
+  cudaEvent_t ev_open = nullptr;
+};
+
+namespace cm {
+
+// Bump-allocates `bytes` (256-byte aligned) from the context workspace for the
+// duration of one entry point.  Returns nullptr if it does not fit.
+void *ws_take(cm_ctx *ctx, size_t bytes);
+// Makes the workspace at least `bytes` large (synchronising the device before
+// replacing a smaller buffer).  Returns a CM status.
+int ws_ensure(cm_ctx *ctx, size_t bytes);
+inline void ws_reset(cm_ctx *ctx) { ctx->ws_used = 0; }
+
+// Stage timing: events recorded on the launch stream around one kernel.
+void stage_begin(cm_ctx *ctx, cudaStream_t s);
+void stage_end(cm_ctx *ctx, int stage, cudaStream_t s);
+
+// Records the CUDA error (if any) as the thread's last error; returns a status.
+int cuda_status(cudaError_t e, const char *what);
+int check_launch(cm_ctx *ctx, const char *what);
+
+// Workspace bytes each stage needs for a graph of n vertices, m entries.
+size_t match_ws_bytes(int64_t n, int64_t m);
+size_t cmap_ws_bytes(int64_t n);
+size_t contract_ws_bytes(int64_t n, int64_t m);
+
+// Stage launchers shared between entry points (no argument checking).
+int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, int32_t *d_match,
+                 cudaStream_t s);
+int launch_cmap(cm_ctx *ctx, int32_t n, const int32_t *xadj, const int32_t *vwgt, const int32_t *match,
+                int32_t *cmap, int32_t *leader, int32_t *cvwgt, int32_t *eoff, int32_t *d_cnvtxs,
+                int32_t *long_list, int32_t long_threshold, int32_t long_chunk, unsigned long long *d_long_ctr,
+                int32_t *chunk_row, int32_t *first_row, int32_t tile_diag, cudaStream_t s);
+int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int32_t *cmap, cm_graph *coarse,
+                    int32_t *d_sizes, cudaStream_t s);
+
+}  // namespace cm

@@ -1,0 +1,204 @@
+/*
+ * cm.h -- C ABI of libcm, the GB300 (sm_103a) multilevel-coarsening library.
+ *
+ * The library rebuilds the coarsening hot path of cuMetis (lancunes/cuMetis):
+ * heavy-edge matching, coarse-vertex map (cmap) construction and graph
+ * contraction (sort of each coarse adjacency row, merge of duplicate edges,
+ * summing of edge weights, coarse CSR emit).  Every entry point is plain C:
+ * int32 CSR arrays, sizes, a status return and an optional CUDA stream passed
+ * as `void *` (a cudaStream_t; NULL = the legacy default stream).
+ *
+ * Reference interfaces replaced (paths inside the cuMetis project):
+ *   cuMetis.cu:1699  int  cuMetis_gpu_match(admin, graph, level)      -> cm_match + cm_build_cmap
+ *   cuMetis.cu:1291  void cuMetis_gpu_create_cgraph(admin, graph, ..)  -> cm_contract
+ *   cuMetis.cu:1824  cuMetis_graph_t *cuMetis_coarsen(admin, graph)    -> cm_coarsen
+ *   include/cuMetis.h:18, cuMetis.cu:3622  cuMetis_PartGraph(...)      -> cm_part_graph / cuMetis_PartGraph
+ *   cuMetis.cu:3712  cuMetis_readgraph(filename)                       -> cm_read_graph
+ *   cuMetis.cu:3856  cuMetis_writetofile(fname, part, n, nparts)       -> cm_write_partition
+ *   cuMetis.cu:356   cuMetis_computecut(graph, where)                  -> cm_edge_cut
+ *
+ * Conventions
+ *   - Every function returns CM_OK (0) or a CM_ERR_* code; none calls exit().
+ *     cm_last_error() returns a message for the calling thread's last failure.
+ *   - Arrays named d_* are device pointers on the context's device; the
+ *     caller owns them.  Host graphs filled by cm_gen_* / cm_read_graph are
+ *     owned by the library and released with cm_graph_free().
+ *   - No global mutable state: all device workspace lives in a cm_ctx.  A
+ *     context is used by one host thread at a time.
+ */
+#ifndef CM_H_
+#define CM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  CM_OK = 0,
+  CM_ERR_INVALID = 1,     /* bad argument or malformed CSR                    */
+  CM_ERR_NOMEM = 2,       /* host/device allocation failed or budget exceeded */
+  CM_ERR_CUDA = 3,        /* CUDA runtime error (see cm_last_error)           */
+  CM_ERR_LIMIT = 4,       /* a device-side wait or round limit ran out        */
+  CM_ERR_IO = 5,          /* file open / parse error                          */
+  CM_ERR_UNSUPPORTED = 6  /* sizes beyond int32 CSR limits, no GPU, ...       */
+};
+
+/* ---- matching modes ---------------------------------------------------- */
+enum {
+  /* Heavy-edge matching, deterministic: every vertex prefers its heaviest
+   * eligible neighbour, ties to the lower vertex id; conflicts resolved by
+   * mutual-proposal handshakes iterated to a fixed point.  The result equals
+   * the sequential greedy matching over eligible edges sorted by
+   * (weight desc, min endpoint asc, max endpoint asc). */
+  CM_MATCH_HEM = 0,
+  /* Same, but equal weights are ordered by a fixed hash of the edge's
+   * endpoints (fewer handshake rounds on unit-weight meshes). */
+  CM_MATCH_HEM_HASH = 1,
+  /* One unsynchronised proposal pass plus cleanup, like cuMetis.cu:1563-1630;
+   * nondeterministic, always a legal matching. */
+  CM_MATCH_RACY = 2
+};
+
+/* ---- graphs ------------------------------------------------------------ */
+typedef struct cm_graph {
+  int32_t nvtxs;    /* n                                              */
+  int32_t nedges;   /* m = xadj[n], directed adjacency entries (2x undirected) */
+  int32_t *xadj;    /* n+1                                            */
+  int32_t *adjncy;  /* m                                              */
+  int32_t *adjwgt;  /* m                                              */
+  int32_t *vwgt;    /* n                                              */
+} cm_graph;
+
+/* Host graphs (library-allocated; free with cm_graph_free). */
+int  cm_graph_alloc(int32_t nvtxs, int32_t nedges, cm_graph *out);
+void cm_graph_free(cm_graph *g);
+/* Structural check of a host CSR: monotone xadj, ids in range, no self loops
+ * (allowed if allow_self_loops), symmetric adjacency with equal weights. */
+int  cm_graph_validate(const cm_graph *g, int check_symmetry, int allow_self_loops);
+
+/* Synthetic inputs, all int32 CSR with rows sorted by neighbour id. */
+int cm_gen_tri_grid(int32_t nx, int32_t ny, cm_graph *out);  /* right, down, down-right diagonal */
+int cm_gen_grid2d(int32_t nx, int32_t ny, cm_graph *out);    /* 5-point */
+int cm_gen_grid3d(int32_t nx, int32_t ny, int32_t nz, cm_graph *out); /* 7-point */
+/* R-MAT: edge_factor * 2^scale generated pairs, quadrant probabilities a,b,c
+ * (d = 1-a-b-c); self loops and duplicates dropped, symmetrised; edge weights
+ * uniform in [wmin, wmax] (same for both directions); vertex weights 1. */
+int cm_gen_rmat(int32_t scale, int32_t edge_factor, double a, double b, double c,
+                uint64_t seed, int32_t wmin, int32_t wmax, cm_graph *out);
+/* Random geometric graph in the unit square, radius sqrt(mean_degree/(pi n)),
+ * vertices numbered in cell order; unit weights. */
+int cm_gen_rgg(int32_t n, double mean_degree, uint64_t seed, cm_graph *out);
+
+/* METIS .graph IO (formats 0/1/10/11 and the 100s digit, as cuMetis.cu:3712). */
+int cm_read_graph(const char *path, cm_graph *out);
+int cm_write_graph(const char *path, const cm_graph *g);
+/* Writes "<graph_path>.part.<nparts>", one part id per line (cuMetis.cu:3856). */
+int cm_write_partition(const char *graph_path, int32_t nparts, int32_t nvtxs, const int32_t *part);
+/* Edge cut (sum of cut edge weights / 2) and max part weight * nparts / total. */
+int64_t cm_edge_cut(const cm_graph *g, const int32_t *part);
+double  cm_imbalance(const cm_graph *g, int32_t nparts, const int32_t *part);
+
+/* ---- device context ---------------------------------------------------- */
+typedef struct cm_ctx cm_ctx;
+
+int  cm_ctx_create(int device, cm_ctx **out);
+void cm_ctx_destroy(cm_ctx *ctx);
+/* Pre-sizes the context's device workspace for graphs up to n vertices and
+ * m entries, so later calls on such graphs do not allocate. */
+int  cm_ctx_reserve(cm_ctx *ctx, int64_t nvtxs, int64_t nedges);
+const char *cm_last_error(void);
+/* Waits for `stream` and returns the first error a kernel of this context
+ * recorded since the last check (CM_ERR_LIMIT for a timed-out device wait,
+ * CM_ERR_INVALID for an invalid matching), clearing it. */
+int cm_ctx_sync(cm_ctx *ctx, void *stream);
+/* Number of kernels this context has launched since creation. */
+int64_t cm_ctx_launch_count(const cm_ctx *ctx);
+
+/* Per-stage timing with CUDA events recorded around each kernel on the
+ * caller's stream (replaces the reference's cudaDeviceSynchronize +
+ * gettimeofday phase timers, cuMetis.cu:4-144).  cm_ctx_stage_times waits for
+ * the recorded events and writes the accumulated milliseconds of up to `cap`
+ * stages (CM_STAGE_* order); reset != 0 clears the accumulators. */
+enum {
+  CM_STAGE_MATCH = 0, CM_STAGE_CMAP = 1, CM_STAGE_LONG_SORT = 2, CM_STAGE_LONG_MERGE = 3,
+  CM_STAGE_LONG_DEDUP = 4, CM_STAGE_TILES = 5, CM_STAGE_LONG_COPY = 6, CM_STAGE_COUNT = 7
+};
+int cm_ctx_set_stage_timing(cm_ctx *ctx, int enable);
+int cm_ctx_stage_times(cm_ctx *ctx, double *ms, int32_t cap, int reset);
+const char *cm_stage_name(int32_t stage);
+
+/* ---- one coarsening level (device arrays) ------------------------------ */
+/* Heavy-edge matching (replaces cuMetis.cu:1709-1750: initcuda_match,
+ * bb_segsort of each row by weight, cuda_shem2, cuda_cleanv, findc1).
+ * Eligible pair (v,k): v != k, vwgt[v]+vwgt[k] <= maxvwgt and
+ * 3*vwgt[v] < maxvwgt or 3*vwgt[k] < maxvwgt (cuMetis.cu:1570, 1583).
+ * On return d_match[v] = partner, or v for a singleton (match is an
+ * involution).  *rounds_out (optional host pointer) receives the number of
+ * handshake rounds. The fine graph is not modified. */
+int cm_match(cm_ctx *ctx, const cm_graph *g_dev, int32_t maxvwgt, int32_t mode,
+             int32_t *d_match, int32_t *rounds_out, void *stream);
+
+/* Coarse-vertex map (replaces findc2, thrust::inclusive_scan, findc2_5, findc3,
+ * findc4 at cuMetis.cu:1634-1694,1755-1789 and the host exclusive scan at
+ * cuMetis.cu:1304).  Leader = min(v, match[v]); coarse ids are assigned to
+ * leaders in increasing order; d_cmap[v] for all v; d_leader[c] = leader of c;
+ * d_cvwgt[c] = pair weight sum; d_eoff[c] = exclusive prefix of
+ * deg(leader)+deg(follower) (d_eoff[n'] = m); d_cnvtxs[0] = n'.
+ * d_leader, d_cvwgt need n entries, d_eoff n+1. */
+int cm_build_cmap(cm_ctx *ctx, int32_t nvtxs, const int32_t *d_xadj, const int32_t *d_vwgt,
+                  const int32_t *d_match, int32_t *d_cmap, int32_t *d_leader,
+                  int32_t *d_cvwgt, int32_t *d_eoff, int32_t *d_cnvtxs, void *stream);
+
+/* Contraction given a matching (replaces cuMetis_gpu_create_cgraph,
+ * cuMetis.cu:1291-1406, with its bb_segsort and Sort_cnedges2_part1..3).
+ * Output contract: coarse vertex c <-> leader c in increasing leader order;
+ * cvwgt[c] = vwgt[leader] + vwgt[follower]; row c = the entries
+ * (cmap[x], w) of the leader's and the follower's rows, self loops removed,
+ * sorted by coarse id, duplicates merged with weights summed.
+ * `coarse` holds device buffers with capacity n+1 (xadj), n (vwgt) and m
+ * (adjncy, adjwgt); d_cmap receives n entries; d_sizes (device, 2 ints)
+ * receives {n', m'}.  Nothing is read back to the host. */
+int cm_contract(cm_ctx *ctx, const cm_graph *fine_dev, const int32_t *d_match,
+                int32_t *d_cmap, cm_graph *coarse_dev, int32_t *d_sizes, void *stream);
+
+/* ---- multilevel coarsening --------------------------------------------- */
+typedef struct cm_coarsen_params {
+  int32_t coarsen_to;      /* stop when n' <= coarsen_to (Coarsen_threshold)   */
+  int32_t maxvwgt;         /* <= 0: (int)(1.5 * tvwgt / coarsen_to) (cu:1828)   */
+  int32_t match_mode;      /* CM_MATCH_*                                       */
+  int32_t max_levels;      /* safety cap, e.g. 64                              */
+  double  shrink;          /* continue while n' < shrink * n (0.75, cu:1844)   */
+} cm_coarsen_params;
+
+void cm_coarsen_default_params(int32_t nvtxs, int32_t nparts, cm_coarsen_params *p);
+
+typedef struct cm_hierarchy cm_hierarchy;
+
+/* Coarsens a host graph (copied to the device inside the call) or, with
+ * input_on_device != 0, a graph whose arrays are already device pointers.
+ * The hierarchy keeps every level and each level's cmap on the device. */
+int cm_coarsen(cm_ctx *ctx, const cm_graph *g, int input_on_device,
+               const cm_coarsen_params *params, cm_hierarchy **out, void *stream);
+void    cm_hierarchy_free(cm_hierarchy *h);
+int32_t cm_hierarchy_levels(const cm_hierarchy *h);   /* graphs incl. the input */
+/* Device view of level l (0 = input); cmap is NULL for the coarsest level. */
+int cm_hierarchy_level(const cm_hierarchy *h, int32_t level, cm_graph *g_dev,
+                       const int32_t **d_cmap, const int32_t **d_match);
+/* Copies level l to a library-allocated host graph, and optionally its cmap
+ * and matching (n of level l each; not for the coarsest level). */
+int cm_hierarchy_copy_level(const cm_hierarchy *h, int32_t level, cm_graph *out,
+                            int32_t *cmap_host, int32_t *match_host);
+
+/* Copies level l into caller-owned host buffers (n+1, m, m, n entries; sizes
+ * from cm_hierarchy_level), e.g. pinned memory, on the hierarchy's stream. */
+int cm_hierarchy_read_level(const cm_hierarchy *h, int32_t level, int32_t *xadj, int32_t *adjncy,
+                            int32_t *adjwgt, int32_t *vwgt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CM_H_ */

@@ -1,0 +1,298 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle and the
+reference's golden outputs.  Integer work: every comparison is bit-exact."""
+import numpy as np
+import pytest
+
+import cumetis_gb300 as cm
+from conftest import GOLDEN_CASES, load_golden
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _o(g):
+    return O.CSR(g.xadj, g.adjncy, g.adjwgt, g.vwgt)
+
+
+def _h(g):
+    return cm.Graph(g.xadj, g.adjncy, g.adjwgt, g.vwgt)
+
+
+def _dev(g):
+    return _h(g).to_device()
+
+
+def gpu_match(ctx, g, maxvwgt, mode=0):
+    m, rounds = ctx.match(_dev(g), maxvwgt, mode)
+    return m.cpu().numpy(), rounds
+
+
+def gpu_contract(ctx, g, match):
+    import torch
+    dg = _dev(g)
+    cg, cmap = ctx.contract(dg, torch.from_numpy(np.ascontiguousarray(match, np.int32)).cuda())
+    h = cg.to_host()
+    return O.CSR(h.xadj, h.adjncy, h.adjwgt, h.vwgt), cmap.cpu().numpy()
+
+
+def assert_same_graph(a, b, what=""):
+    for f in ("xadj", "adjncy", "adjwgt", "vwgt"):
+        x, y = getattr(a, f), getattr(b, f)
+        assert len(x) == len(y) and np.array_equal(x, y), (what, f)
+
+
+# ---------------------------------------------------------------------------
+def star(n_leaves, w=1):
+    xadj = [0, n_leaves] + [n_leaves + i + 1 for i in range(n_leaves)]
+    adj = list(range(1, n_leaves + 1)) + [0] * n_leaves
+    wt = [(i % 97) + w for i in range(n_leaves)] * 2
+    return O.CSR(xadj, adj, wt, [1] * (n_leaves + 1))
+
+
+def clique(k):
+    xadj, adj = [0], []
+    for v in range(k):
+        adj += [u for u in range(k) if u != v]
+        xadj.append(len(adj))
+    w = [1 + ((min(v, u) * 31 + max(v, u)) % 5) for v in range(k) for u in range(k) if u != v]
+    return O.CSR(xadj, adj, w, [1] * k)
+
+
+def synthetic_graphs():
+    gs = {
+        "tri69": _o(cm.gen_tri_grid(69, 69)),
+        "grid2d_100": _o(cm.gen_grid2d(100, 100)),
+        "grid3d_16": _o(cm.gen_grid3d(16, 16, 16)),
+        "rmat14": _o(cm.gen_rmat(14, 16, seed=11)),
+        "rgg20k": _o(cm.gen_rgg(20000, 8.0, seed=3)),
+        "star5000": star(5000),
+        "clique60": clique(60),
+        "path": O.CSR(np.r_[0, np.arange(1, 2 * 999, 2), 2 * 999], np.array(
+            [1] + [x for v in range(1, 999) for x in (v - 1, v + 1)] + [998], np.int32), np.ones(2 * 999, np.int32),
+            np.ones(1000, np.int32)),
+        "isolated": O.CSR(np.zeros(101, np.int32), np.zeros(0, np.int32), np.zeros(0, np.int32),
+                          np.ones(100, np.int32)),
+    }
+    # heavy vertex weights: the light rule and the cap both bind
+    g = cm.gen_grid2d(60, 60)
+    gs["vw_grid"] = O.CSR(g.xadj, g.adjncy, g.adjwgt, (1 + (np.arange(g.nvtxs) * 13) % 11).astype(np.int32))
+    return gs
+
+
+@pytest.fixture(scope="module")
+def graphs():
+    return synthetic_graphs()
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_match_bitexact_synthetic(ctx, graphs, mode):
+    for name, g in graphs.items():
+        for mv in (O.maxvwgt_rule(int(g.vwgt.sum()), 100), 3, 29):
+            want = O.match_greedy(g, mv, mode)
+            got, rounds = gpu_match(ctx, g, mv, mode)
+            assert np.array_equal(got, want), (name, mv, mode)
+            code, bad, maximal = O.check_matching(g, mv, got)
+            assert code == 0 and maximal
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_match_bitexact_on_golden_levels(ctx, name):
+    """Inputs with hash-ordered rows and summed weights (the reference's own
+    coarse graphs) as well as the original graph."""
+    G = load_golden(name)
+    maxvwgt, graphs, _ = G["seeds"][1]
+    for l, g in enumerate(graphs):
+        for mode in (0, 1):
+            want = O.match_greedy(g, maxvwgt, mode)
+            got, _ = gpu_match(ctx, g, maxvwgt, mode)
+            assert np.array_equal(got, want), (name, l, mode)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_contract_bitexact_vs_reference(ctx, name):
+    """Given the reference's own matching at every level, the CUDA contraction
+    reproduces the reference's cmap, vertex weights and coarse adjacency
+    (rows sorted by coarse id, as the reference's GPU path emits them)."""
+    G = load_golden(name)
+    for seed, (maxvwgt, graphs, cmaps) in G["seeds"].items():
+        for l, cmap in enumerate(cmaps):
+            match = O.match_from_cmap(cmap)
+            cg, gcmap = gpu_contract(ctx, graphs[l], match)
+            assert np.array_equal(gcmap, cmap), (name, seed, l)
+            ref = graphs[l + 1]
+            ra, rw = ref.rows_sorted()
+            assert np.array_equal(cg.xadj, ref.xadj), (name, seed, l)
+            assert np.array_equal(cg.adjncy, ra) and np.array_equal(cg.adjwgt, rw), (name, seed, l)
+            assert np.array_equal(cg.vwgt, ref.vwgt)
+
+
+def test_contract_bitexact_vs_oracle(ctx, graphs):
+    for name, g in graphs.items():
+        match = O.match_greedy(g, O.maxvwgt_rule(int(g.vwgt.sum()), 100), 0)
+        want, wcmap = O.contract(g, match)
+        got, gcmap = gpu_contract(ctx, g, match)
+        assert np.array_equal(gcmap, wcmap), name
+        assert_same_graph(got, want, name)
+
+
+def _long_row_graph(L_leader, L_follower, extra=0, seed=0):
+    """A pair (0,1) whose expanded coarse row has L_leader + L_follower
+    entries, with overlapping neighbourhoods (duplicates to merge), plus
+    `extra` matched pairs among the leaves."""
+    rng = np.random.default_rng(seed)
+    nleaf = max(L_leader, L_follower) + 8
+    n = 2 + nleaf
+    edges = {(0, 1)}
+    a = rng.choice(np.arange(2, n), L_leader - 1, replace=False)
+    b = rng.choice(np.arange(2, n), L_follower - 1, replace=False)
+    edges |= {(0, int(x)) for x in a} | {(1, int(x)) for x in b}
+    for i in range(extra):
+        u, v = 2 + 2 * i, 3 + 2 * i
+        if v < n:
+            edges.add((u, v))
+    src = np.array([e[0] for e in edges] + [e[1] for e in edges])
+    dst = np.array([e[1] for e in edges] + [e[0] for e in edges])
+    lo, hi = np.minimum(src, dst), np.maximum(src, dst)
+    w = 1 + (lo * 7 + hi * 13) % 50
+    order = np.lexsort((dst, src))
+    src, dst, w = src[order], dst[order], w[order]
+    xadj = np.zeros(n + 1, np.int64)
+    np.add.at(xadj, src + 1, 1)
+    return O.CSR(np.cumsum(xadj), dst, w, np.ones(n))
+
+
+@pytest.mark.parametrize("lens", [(1024, 1024), (1024, 1025), (4096, 4096), (4097, 4096), (20000, 13000),
+                                  (40000, 30000)])
+def test_long_rows(ctx, lens):
+    """Coarse rows around and far beyond the tile limit (2048) and the
+    long-row chunk (8192): exercises chunk sort, merge passes, dedup, copy."""
+    g = _long_row_graph(*lens, extra=500, seed=sum(lens))
+    match = np.arange(g.n, dtype=np.int32)
+    match[0], match[1] = 1, 0
+    for i in range(500):
+        u, v = 2 + 2 * i, 3 + 2 * i
+        if v < g.n:
+            match[u], match[v] = v, u
+    want, wcmap = O.contract(g, match)
+    got, gcmap = gpu_contract(ctx, g, match)
+    assert np.array_equal(gcmap, wcmap)
+    assert_same_graph(got, want, str(lens))
+
+
+def test_many_long_rows(ctx):
+    """Many hubs at once (R-MAT skew at a size the oracle finishes quickly)."""
+    g = _o(cm.gen_rmat(16, 32, a=0.6, b=0.15, c=0.15, seed=5))
+    match = O.match_greedy(g, O.maxvwgt_rule(int(g.vwgt.sum()), 1000), 0)
+    want, wcmap = O.contract(g, match)
+    got, gcmap = gpu_contract(ctx, g, match)
+    assert np.array_equal(gcmap, wcmap)
+    assert_same_graph(got, want, "rmat16")
+
+
+def test_build_cmap(ctx, graphs):
+    import torch
+    for name, g in graphs.items():
+        match = O.match_greedy(g, O.maxvwgt_rule(int(g.vwgt.sum()), 100), 0)
+        cmap, leader, cvwgt, eoff = O.build_cmap(g, match)
+        gc, gl, gv, ge, cn = ctx.build_cmap(_dev(g), torch.from_numpy(match).cuda())
+        assert cn == len(leader), name
+        assert np.array_equal(gc.cpu().numpy(), cmap)
+        assert np.array_equal(gl.cpu().numpy(), leader)
+        assert np.array_equal(gv.cpu().numpy(), cvwgt)
+        assert np.array_equal(ge.cpu().numpy(), eoff)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_coarsen_hierarchy_bitexact(ctx, mode):
+    """The whole multilevel loop (stop rule of cuMetis.cu:1843) against the
+    oracle's level loop: every level's graph, matching and cmap."""
+    for g, thr in ((cm.gen_tri_grid(69, 69), 100), (cm.gen_tri_grid(69, 69), 240), (cm.gen_grid2d(200, 150), 500),
+                   (cm.gen_rmat(13, 16, seed=4), 200), (cm.gen_rgg(30000, 8.0, seed=9), 300)):
+        want = O.coarsen(_o(g), thr, mode)
+        h = ctx.coarsen(g, thr, mode)
+        assert len(h) == len(want), (len(h), len(want))
+        for l, (wg, wm, wc) in enumerate(want):
+            hg, hc, hm = h.copy_level(l)
+            assert_same_graph(_o(hg), wg, "level %d" % l)
+            if wm is not None:
+                assert np.array_equal(hm, wm) and np.array_equal(hc, wc), l
+        h.close()
+
+
+def test_coarsen_device_input(ctx):
+    g = cm.gen_grid3d(20, 20, 20)
+    want = O.coarsen(_o(g), 300)
+    h = ctx.coarsen(g.to_device(), 300)
+    assert [s[0] for s in h.sizes()] == [lv[0].n for lv in want]
+    hg, _, _ = h.copy_level(len(h) - 1)
+    assert_same_graph(_o(hg), want[-1][0])
+
+
+def test_invalid_match_reported(ctx):
+    import torch
+    g = _o(cm.gen_grid2d(10, 10))
+    bad = np.arange(g.n, dtype=np.int32)
+    bad[0] = 1  # 0 -> 1 but 1 -> 1: not an involution
+    with pytest.raises(cm.CMError) as e:
+        ctx.contract(_dev(g), torch.from_numpy(bad).cuda())
+    assert e.value.code == cm.CM_ERR_INVALID
+    # the context stays usable
+    m = O.match_greedy(g, 10, 0)
+    got, _ = gpu_contract(ctx, g, m)
+    want, _ = O.contract(g, m)
+    assert_same_graph(got, want)
+
+
+def test_empty_and_tiny(ctx):
+    for g in (O.CSR([0], [], [], []), O.CSR([0, 0], [], [], [1]), O.CSR([0, 1, 2], [1, 0], [3, 3], [1, 1])):
+        mv = 10
+        got, _ = gpu_match(ctx, g, mv)
+        assert np.array_equal(got, O.match_greedy(g, mv, 0))
+        if g.n:
+            cg, cmap = gpu_contract(ctx, g, got)
+            want, wc = O.contract(g, got)
+            assert_same_graph(cg, want)
+
+
+# ---------------------------------------------------------------------------
+# full-size workloads: bit-exact where the oracle finishes in seconds, and
+# size-independent properties otherwise
+def test_grid725_full_size_bitexact(ctx):
+    g = cm.gen_grid2d(725, 725)
+    thr = cm.coarsen_threshold(g.nvtxs, 64)
+    want = O.coarsen(_o(g), thr)
+    h = ctx.coarsen(g, thr)
+    assert len(h) == len(want)
+    for l, (wg, wm, wc) in enumerate(want):
+        hg, hc, hm = h.copy_level(l)
+        assert_same_graph(_o(hg), wg, "level %d" % l)
+        if wm is not None:
+            assert np.array_equal(hm, wm)
+
+
+def test_rmat22_full_size(ctx):
+    """R-MAT scale 22 (the throughput workload): matching bit-exact against
+    the oracle; contraction checked by invariants (total vertex weight,
+    total edge weight minus the matched pairs' internal edges, sorted unique
+    symmetric rows) and bit-exact against the oracle's contraction."""
+    g = cm.gen_rmat(22, 16, seed=1)
+    thr = cm.coarsen_threshold(g.nvtxs, 256)
+    mv = cm.maxvwgt_rule(g.nvtxs, thr)
+    og = _o(g)
+    dg = g.to_device()
+    m, rounds = ctx.match(dg, mv, 0)
+    got = m.cpu().numpy()
+    want = O.match_greedy(og, mv, 0)
+    assert np.array_equal(got, want)
+    cg, cmap = ctx.contract(dg, m)
+    h = cg.to_host()
+    assert h.vwgt.sum() == g.vwgt.sum()
+    row = np.repeat(np.arange(g.nvtxs), np.diff(g.xadj))
+    internal = got[row] == g.adjncy
+    assert int(h.adjwgt.astype(np.int64).sum()) == int(g.adjwgt[~internal].astype(np.int64).sum())
+    d = np.diff(h.adjncy)
+    crow = np.repeat(np.arange(h.nvtxs), np.diff(h.xadj))
+    assert np.all((d > 0) | (np.diff(crow) > 0))
+    wcg, wcmap = O.contract(og, want)
+    assert np.array_equal(cmap.cpu().numpy(), wcmap)
+    assert_same_graph(_o(h), wcg, "rmat22")
