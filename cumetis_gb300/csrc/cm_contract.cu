@@ -33,19 +33,50 @@ namespace {
 
 constexpr int kTileThreads = 256;
 constexpr int kTileE = 8;
-constexpr int kTileDiag = 1024;                   // D
+constexpr int kTileDiag = 512;                    // D
 constexpr int kLongThr = 2048;                    // rows longer than this take the long path
 constexpr int kTileCap = kTileDiag + kLongThr;    // max entries in a tile (multiple of kTileE)
 constexpr int kChunk = 8192;                      // long-row chunk (entries sorted per block)
 constexpr int kChunkThreads = 512;
 constexpr unsigned kSelfKey = 0xffffffffu;        // self loops sort last in their row
 
+// Composite sort key (tile-local row, coarse id).  32-bit when coarse ids fit
+// in 23 bits (n < 2^23 - 1; rows need 9 bits for kTileDiag = 512), else 64-bit.  The self-loop id is the largest
+// id value, so self loops sort last in their row; the pad sorts after all.
+template <typename K> struct KeyT;
+template <> struct KeyT<unsigned> {
+  static constexpr int kShift = 23;
+  static constexpr unsigned kIdMask = (1u << 23) - 1;
+  static constexpr unsigned kSelf = kIdMask;
+  static constexpr unsigned kPad = 0xffffffffu;
+  static __device__ __forceinline__ unsigned make(int r, unsigned id) { return ((unsigned)r << kShift) | id; }
+  static __device__ __forceinline__ int row(unsigned k) { return (int)(k >> kShift); }
+  static __device__ __forceinline__ unsigned id(unsigned k) { return k & kIdMask; }
+};
+template <> struct KeyT<unsigned long long> {
+  static constexpr unsigned kSelf = 0xffffffffu;
+  static constexpr unsigned long long kPad = ~0ull;
+  static __device__ __forceinline__ unsigned long long make(int r, unsigned id) {
+    return ((unsigned long long)r << 32) | id;
+  }
+  static __device__ __forceinline__ int row(unsigned long long k) { return (int)(k >> 32); }
+  static __device__ __forceinline__ unsigned id(unsigned long long k) { return (unsigned)k; }
+};
+constexpr int kSmallIdLimit = (1 << 23) - 1;   // n below this uses 32-bit keys
+static_assert(kTileDiag <= 512, "tile rows must fit in 9 bits");
+
+template <typename K>
 struct TileSmem {
-  unsigned long long ck[2][kTileCap];
-  int cw[2][kTileCap];
+  // k0/w0: gathered entries; k1/w1: sort scratch, and before the sort the
+  // hash table that counts unique (row, id) keys (contiguous: 12 or 8 bytes
+  // per tile entry).
+  K k0[kTileCap];
+  int w0[kTileCap];
+  K k1[kTileCap];
+  int w1[kTileCap];
   int r_xl[kTileDiag], r_dl[kTileDiag], r_xf[kTileDiag], r_start[kTileDiag], r_len[kTileDiag], r_c[kTileDiag];
   int scan[kTileThreads / 32 + 1];
-  int s_tile, s_clo, s_chi, s_ntot;
+  int s_tile, s_clo, s_chi;
   unsigned long long s_base;
 };
 
@@ -63,14 +94,16 @@ __device__ __forceinline__ int upper_bound_smem(const int *a, int n, int x) {
 // (as find_cnvtxsedge_original places them, cuMetis.cu:1014-1020).
 __device__ __forceinline__ int expanded_src(int o, int xl, int dl, int xf) { return o < dl ? xl + o : xf + (o - dl); }
 
-__global__ void __launch_bounds__(kTileThreads, 2)
+template <typename K>
+__global__ void __launch_bounds__(kTileThreads, sizeof(K) == 4 ? 4 : 2)
 k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
                  const int *__restrict__ match, const int *__restrict__ cmap, const int *__restrict__ leader,
-                 const int *__restrict__ eoff, const int *__restrict__ d_cn, const int *__restrict__ first_row,
+                 const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
                  const int *__restrict__ ucount, unsigned long long *lb, int *__restrict__ cxadj,
-                 int *__restrict__ cadjncy, int *__restrict__ cadjwgt, int *__restrict__ d_sizes, DevStatus *st) {
+                 int *__restrict__ cadjncy, int *__restrict__ cadjwgt, int *d_sizes, DevStatus *st) {
+  using KT = KeyT<K>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  TileSmem &S = *reinterpret_cast<TileSmem *>(smem_raw);
+  TileSmem<K> &S = *reinterpret_cast<TileSmem<K> *>(smem_raw);
   const int tid = threadIdx.x;
   const int nc = *d_cn;
   const long long m = eoff[nc];
@@ -90,7 +123,7 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
     R = 0;
   }
 
-  // Row metadata; per-thread chunks of consecutive rows for the length scan.
+  // Row metadata: 4 consecutive rows per thread (independent load chains).
   constexpr int kRowsPerThread = kTileDiag / kTileThreads;
   int lens[kRowsPerThread];
   int mysum = 0;
@@ -129,41 +162,89 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
   }
   __syncthreads();
 
-  // Gather (row, cmap[x]) keys and weights; consecutive entries of a fine row
-  // map to consecutive lanes (coalesced adjncy/adjwgt reads).
-  for (int e = tid; e < ntot; e += kTileThreads) {
-    const int r = upper_bound_smem(S.r_start, R, e) - 1;
-    const int o = e - S.r_start[r];
-    const int src = expanded_src(o, S.r_xl[r], S.r_dl[r], S.r_xf[r]);
-    const int x = adjncy[src];
-    const int w = adjwgt[src];
-    const int k = cmap[x];
-    const unsigned key = (k == clo + r) ? kSelfKey : (unsigned)k;
-    S.ck[0][e] = ((unsigned long long)r << 32) | key;
-    S.cw[0][e] = w;
+  // Gather (row, cmap[x]) keys and weights, 4 entries in flight per thread;
+  // consecutive entries of a fine row go to consecutive lanes (coalesced).
+  for (int e0 = tid; e0 < ntot; e0 += 4 * kTileThreads) {
+    int src[4], rr[4], x[4], w[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = e0 + u * kTileThreads;
+      rr[u] = 0;
+      src[u] = -1;
+      if (e < ntot) {
+        const int r = upper_bound_smem(S.r_start, R, e) - 1;
+        rr[u] = r;
+        src[u] = expanded_src(e - S.r_start[r], S.r_xl[r], S.r_dl[r], S.r_xf[r]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      x[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
+      w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = e0 + u * kTileThreads;
+      if (e < ntot) {
+        const unsigned id = (x[u] == clo + rr[u]) ? KT::kSelf : (unsigned)x[u];
+        S.k0[e] = KT::make(rr[u], id);
+        S.w0[e] = w[u];
+      }
+    }
+  }
+  // Count unique non-self keys with a shared-memory hash set, so that the
+  // tile's aggregate is published before the (longer) sort: later tiles never
+  // wait on this tile's sort in their look-back.
+  constexpr int kHash = (int)((sizeof(K) + 4) * kTileCap / sizeof(K));
+  K *tab = S.k1;
+  for (int i = tid; i < kHash; i += kTileThreads) tab[i] = KT::kPad;
+  int long_sum = 0;
+#pragma unroll
+  for (int i = 0; i < kRowsPerThread; ++i) {
+    const int r = tid * kRowsPerThread + i;
+    if (r < R && S.r_len[r] < 0) long_sum += ucount[clo + r];
   }
   __syncthreads();
-  const int b = block_merge_sort<unsigned long long, kTileThreads, kTileE>(S.ck[0], S.cw[0], S.ck[1], S.cw[1], ntot,
-                                                                         ~0ull);
-  const unsigned long long *K = S.ck[b];
-  const int *W = S.cw[b];
-  int *hs = reinterpret_cast<int *>(S.ck[b ^ 1]);  // head-count scan, ntot + 1 ints
-
-  // Heads: first of a run of equal (row, id) that is not a self loop.
-  int carry = 0;
-  for (int base = 0; base < ntot; base += kTileThreads) {
-    const int i = base + tid;
-    int h = 0;
-    if (i < ntot) {
-      const unsigned long long k = K[i];
-      h = ((unsigned)k != kSelfKey) && (i == 0 || K[i - 1] != k);
+  int uniq = long_sum;
+  for (int e = tid; e < ntot; e += kTileThreads) {
+    const K key = S.k0[e];
+    if (KT::id(key) == KT::kSelf) continue;
+    unsigned h = (unsigned)(((unsigned long long)key * 0x9E3779B97F4A7C15ull) >> 32) % (unsigned)kHash;
+    for (int probe = 0; probe < kHash; ++probe) {
+      const K old = atomicCAS(&tab[h], KT::kPad, key);
+      if (old == KT::kPad) { ++uniq; break; }
+      if (old == key) break;
+      h = h + 1 == (unsigned)kHash ? 0u : h + 1;
     }
-    int tot;
-    const int e = block_exclusive_scan<kTileThreads>(h, S.scan, &tot);
-    if (i < ntot) hs[i] = carry + e;
-    carry += tot;
   }
-  if (tid == 0) hs[ntot] = carry;
+  int agg;
+  block_exclusive_scan<kTileThreads>(uniq, S.scan, &agg);
+  if (tid < 32) lookback_publish(lb, tile, (unsigned long long)agg);
+  __syncthreads();
+  const int b = block_merge_sort<K, kTileThreads, kTileE>(S.k0, S.w0, S.k1, S.w1, ntot, KT::kPad);
+  const K *Ks = b ? S.k1 : S.k0;
+  const int *W = b ? S.w1 : S.w0;
+  int *hs = reinterpret_cast<int *>(b ? S.k0 : S.k1);  // exclusive head count, ntot + 1 ints
+
+  // Heads (first of a run of equal (row, id), not a self loop): one block scan
+  // over per-thread contiguous chunks.
+  const int ipt = (ntot + kTileThreads - 1) / kTileThreads;
+  const int i0 = min(ntot, tid * ipt), i1 = min(ntot, i0 + ipt);
+  int hcnt = 0;
+  for (int i = i0; i < i1; ++i) {
+    const K k = Ks[i];
+    hcnt += (KT::id(k) != KT::kSelf) && (i == 0 || Ks[i - 1] != k);
+  }
+  int htot;
+  int run = block_exclusive_scan<kTileThreads>(hcnt, S.scan, &htot);
+  for (int i = i0; i < i1; ++i) {
+    const K k = Ks[i];
+    hs[i] = run;
+    run += (KT::id(k) != KT::kSelf) && (i == 0 || Ks[i - 1] != k);
+  }
+  if (tid == 0) hs[ntot] = htot;
   __syncthreads();
 
   // Unique count per row (long rows: from the long-row pass), then row scan.
@@ -182,8 +263,9 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
   }
   int ttot;
   int cex = block_exclusive_scan<kTileThreads>(csum, S.scan, &ttot);
+  if (ttot != agg && tid == 0) record_error(st, CM_ERR_INVALID, ERR_SITE_BOUNDS);  // count paths disagree
   if (tid < 32) {
-    const unsigned long long base = lookback_exclusive(lb, tile, (unsigned long long)ttot, st);
+    const unsigned long long base = lookback_resolve(lb, tile, (unsigned long long)agg, st);
     if (tid == 0) S.s_base = base;
   }
 #pragma unroll
@@ -203,12 +285,12 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
   for (int i = tid; i < ntot; i += kTileThreads) {
     const int hb = hs[i];
     if (hs[i + 1] == hb) continue;  // not a head
-    const unsigned long long k = K[i];
-    const int r = (int)(k >> 32);
+    const K k = Ks[i];
+    const int r = KT::row(k);
     unsigned sum = (unsigned)W[i];
-    for (int j = i + 1; j < ntot && K[j] == k; ++j) sum += (unsigned)W[j];
+    for (int j = i + 1; j < ntot && Ks[j] == k; ++j) sum += (unsigned)W[j];
     const long long pos = base + S.r_c[r] + (hb - hs[S.r_start[r]]);
-    cadjncy[pos] = (int)(unsigned)k;
+    cadjncy[pos] = (int)KT::id(k);
     cadjwgt[pos] = (int)sum;
   }
   if (tid == 0 && (long long)tile * kTileDiag <= dend && dend < (long long)(tile + 1) * kTileDiag) {
@@ -261,11 +343,28 @@ k_long_sort(const int *__restrict__ xadj, const int *__restrict__ adjncy, const 
     const int j = q - long_list[2 * idx + 1];
     const int cs = j * kChunk;
     const int cnt = min(kChunk, L - cs);
-    for (int t = threadIdx.x; t < cnt; t += kChunkThreads) {
-      const int src = expanded_src(cs + t, xl, dl, xf);
-      const int k = cmap[adjncy[src]];
-      S.k[0][t] = k == c ? kSelfKey : (unsigned)k;
-      S.w[0][t] = adjwgt[src];
+    for (int t0 = threadIdx.x; t0 < cnt; t0 += 4 * kChunkThreads) {
+      int src[4], x[4], w[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int t = t0 + u * kChunkThreads;
+        src[u] = t < cnt ? expanded_src(cs + t, xl, dl, xf) : -1;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        x[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
+        w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int t = t0 + u * kChunkThreads;
+        if (t < cnt) {
+          S.k[0][t] = x[u] == c ? kSelfKey : (unsigned)x[u];
+          S.w[0][t] = w[u];
+        }
+      }
     }
     __syncthreads();
     const int b = block_merge_sort<unsigned, kChunkThreads, 8>(S.k[0], S.w[0], S.k[1], S.w[1], cnt, kSelfKey);
@@ -448,8 +547,14 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
                        kTileDiag, s);
   if (rc) return rc;
   const int persistent = ctx->num_sms;
-  const size_t tile_smem = sizeof(TileSmem), chunk_smem = sizeof(ChunkSmem);
-  cudaFuncSetAttribute(k_contract_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem);
+  const bool small_ids = n < kSmallIdLimit;
+  const size_t tile_smem = small_ids ? sizeof(TileSmem<unsigned>) : sizeof(TileSmem<unsigned long long>);
+  const size_t chunk_smem = sizeof(ChunkSmem);
+  if (small_ids)
+    cudaFuncSetAttribute(k_contract_tiles<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem);
+  else
+    cudaFuncSetAttribute(k_contract_tiles<unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tile_smem);
   cudaFuncSetAttribute(k_long_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chunk_smem);
   stage_begin(ctx, s);
   k_long_sort<<<persistent, kChunkThreads, chunk_smem, s>>>(fine->xadj, fine->adjncy, fine->adjwgt, match, cmap,
@@ -479,9 +584,14 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   ctx->launches++;
   // d_sizes[0] temporarily holds n' (written by the cmap scan).
   stage_begin(ctx, s);
-  k_contract_tiles<<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
-      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, d_sizes, first_row, ucount, lb,
-      coarse->xadj, coarse->adjncy, coarse->adjwgt, d_sizes, st);
+  if (small_ids)
+    k_contract_tiles<unsigned><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
+        fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, d_sizes, first_row, ucount, lb,
+        coarse->xadj, coarse->adjncy, coarse->adjwgt, d_sizes, st);
+  else
+    k_contract_tiles<unsigned long long><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
+        fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, d_sizes, first_row, ucount, lb,
+        coarse->xadj, coarse->adjncy, coarse->adjwgt, d_sizes, st);
   stage_end(ctx, CM_STAGE_TILES, s);
   ctx->launches++;
   stage_begin(ctx, s);

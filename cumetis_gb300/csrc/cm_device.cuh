@@ -129,18 +129,21 @@ constexpr unsigned long long kLbFlagAgg = 1ull << 62;
 constexpr unsigned long long kLbFlagInc = 2ull << 62;
 constexpr unsigned long long kLbValMask = (1ull << 62) - 1;
 
-// Called by one full warp of the tile's block.  Publishes `aggregate` for
-// tile `tile` and returns the exclusive prefix of all earlier tiles (0 for
-// tile 0).  On a timed-out wait it records CM_ERR_LIMIT and returns 0.
-__device__ __forceinline__ unsigned long long lookback_exclusive(unsigned long long *status, int tile,
-                                                                 unsigned long long aggregate, DevStatus *st) {
+// Publishes tile `tile`'s aggregate (lane 0 of the calling warp).  Tile 0
+// publishes its inclusive prefix directly.
+__device__ __forceinline__ void lookback_publish(unsigned long long *status, int tile, unsigned long long aggregate) {
+  unsigned long long *ts = status + 1;
+  if ((threadIdx.x & 31) == 0) st_release64(&ts[tile], (tile == 0 ? kLbFlagInc : kLbFlagAgg) | aggregate);
+}
+
+// Called by one full warp after lookback_publish: returns the exclusive
+// prefix of all earlier tiles and publishes this tile's inclusive prefix.  On
+// a timed-out wait it records CM_ERR_LIMIT and returns 0.
+__device__ __forceinline__ unsigned long long lookback_resolve(unsigned long long *status, int tile,
+                                                               unsigned long long aggregate, DevStatus *st) {
   const int lane = threadIdx.x & 31;
   unsigned long long *ts = status + 1;
-  if (tile == 0) {
-    if (lane == 0) st_release64(&ts[0], kLbFlagInc | aggregate);
-    return 0;
-  }
-  if (lane == 0) st_release64(&ts[tile], kLbFlagAgg | aggregate);
+  if (tile == 0) return 0;
   unsigned long long excl = 0;
   int idx = tile - 1;
   const uint64_t t0 = global_timer_ns();
@@ -148,7 +151,11 @@ __device__ __forceinline__ unsigned long long lookback_exclusive(unsigned long l
     const int j = idx - lane;
     unsigned long long s = j >= 0 ? ld_acquire64(&ts[j]) : kLbFlagInc;
     unsigned flag = (unsigned)(s >> 62);
-    if (__any_sync(0xffffffffu, flag == 0)) {
+    // Only the predecessors up to the nearest published inclusive prefix are
+    // needed; wait while one of those has not published anything yet.
+    const unsigned inc_mask = __ballot_sync(0xffffffffu, flag == 2);
+    const int last = inc_mask ? (__ffs(inc_mask) - 1) : 31;
+    if (__any_sync(0xffffffffu, lane <= last && flag == 0)) {
       if (global_timer_ns() - t0 > kWaitLimitNs) {
         if (lane == 0) record_error(st, CM_ERR_LIMIT, ERR_SITE_LOOKBACK);
         excl = 0;
@@ -156,9 +163,7 @@ __device__ __forceinline__ unsigned long long lookback_exclusive(unsigned long l
       }
       continue;
     }
-    unsigned inc_mask = __ballot_sync(0xffffffffu, flag == 2);
     unsigned long long v = s & kLbValMask;
-    int last = inc_mask ? (__ffs(inc_mask) - 1) : 31;
     unsigned long long part = lane <= last ? v : 0ull;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
@@ -168,6 +173,13 @@ __device__ __forceinline__ unsigned long long lookback_exclusive(unsigned long l
   }
   if (lane == 0) st_release64(&ts[tile], kLbFlagInc | ((excl + aggregate) & kLbValMask));
   return excl;
+}
+
+// Both steps at once, for tiles whose aggregate is ready only at the end.
+__device__ __forceinline__ unsigned long long lookback_exclusive(unsigned long long *status, int tile,
+                                                                 unsigned long long aggregate, DevStatus *st) {
+  lookback_publish(status, tile, aggregate);
+  return lookback_resolve(status, tile, aggregate, st);
 }
 
 // Inclusive warp scan of 64-bit values.

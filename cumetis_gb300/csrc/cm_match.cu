@@ -10,20 +10,21 @@
 // to the lower vertex id (CM_MATCH_HEM) or to the lower edge hash
 // (CM_MATCH_HEM_HASH, then lower id).  Both orders are strict total orders on
 // edges, so mutual-proposal rounds converge to the unique greedy matching of
-// that order, independent of scheduling.
+// that order whatever the schedule.
 //
-// One persistent cooperative kernel runs all rounds.  A round is two phases
-// separated by grid barriers:
-//   A  every frontier vertex recomputes ptr[v] = its best candidate
-//      (m2[] frozen);
-//   B  mutual pointers commit (m2[v]=p, m2[p]=v); the neighbours x of each
-//      newly matched pair with ptr[x] in the pair join the next frontier
-//      (ptr[] frozen).
+// One persistent cooperative kernel (one 1024-thread block per SM) runs all
+// rounds.  A round has three phases separated by grid barriers:
+//   A  (m2[] frozen)  every vertex of the round's work recomputes ptr[v], its
+//      best candidate.  Rows of <= kSerialDeg entries: one lane each.  Longer
+//      rows: kChunk-entry chunks, one warp each (edge-balanced across the
+//      grid); the last chunk of a row to finish reduces the chunk bests.
+//   B  (ptr[] frozen) mutual pointers commit (m2[v]=p, m2[p]=v).  A pair whose
+//      two rows are short wakes its neighbours x with ptr[x] in the pair at
+//      once; longer pairs queue their rows as wake chunks.
+//   C  wake chunks: neighbours with ptr[x] in the pair join the next round.
 // Vertices whose candidate is still unmatched keep their pointer and wait.
-// m2[v] < 0 encodes "unmatched, vwgt = -1 - m2[v]", so one 4-byte gather per
+// m2[v] < 0 encodes "unmatched, vwgt = -1 - m2[v]": one 4-byte gather per
 // neighbour answers both "matched?" and the weight cap.
-// Lanes handle one frontier vertex each when its row has <= kSerialDeg
-// entries; longer rows are scanned by the whole warp (coalesced loads).
 #include <climits>
 
 #include "cm_ctx.h"
@@ -31,19 +32,29 @@
 namespace cm {
 namespace {
 
-constexpr int kMatchThreads = 256;
-constexpr int kSerialDeg = 16;
+constexpr int kMatchThreads = 1024;
+constexpr int kSerialDeg = 16;   // rows scanned by one lane
+constexpr int kChunk = 256;      // entries per warp work item
+
+struct Slot {      // work of one round (double-buffered by round parity)
+  int *small;      // vertices with rows <= kSerialDeg
+  int *big_v, *big_base, *big_done;  // longer rows, first chunk index, chunks done
+  int *big_map;    // chunk -> index into big_v
+};
 
 struct MatchArgs {
   int n;
   const int *xadj, *adjncy, *adjwgt, *vwgt;
   long long maxvwgt;
   int mode;
-  int *m2;      // result (the caller's match array, used as working state)
-  int *ptr;     // current candidate of every vertex
-  int *stamp;   // last round whose frontier holds the vertex
-  int *fr[2];   // frontiers of odd/even rounds (round 0 is all vertices)
-  int *ctr;     // ctr[0], ctr[1]: frontier sizes
+  int *m2, *ptr, *stamp;
+  Slot slot[2];
+  int *wk_x, *wk_v, *wk_p, *wk_base, *wk_map;   // wake items of the current round
+  int *nsmall;                   // nsmall[0..1]
+  unsigned long long *big;       // big[0..1] = (rows << 32 | chunks)
+  unsigned long long *wk;        // (items << 32 | chunks)
+  int *part_w, *part_k;          // per chunk partial best
+  unsigned *part_h;
   int max_rounds;
   DevStatus *st;
 };
@@ -62,23 +73,40 @@ __device__ __forceinline__ bool better(const Cand &a, const Cand &b) {
   return a.k < b.k;
 }
 
-__device__ __forceinline__ void consider(const MatchArgs &a, int v, long long vw, int j, Cand &best) {
-  const int k = a.adjncy[j];
-  if (k == v) return;
-  const int s = __ldcg(a.m2 + k);
-  if (s >= 0) return;  // matched
+__device__ __forceinline__ void eval(const MatchArgs &a, int v, long long vw, int k, int w, int s, Cand &best) {
+  if (k == v || s >= 0) return;  // self or matched
   const long long vk = -1ll - s;
   if (vw + vk > a.maxvwgt) return;
   if (!(3 * vw < a.maxvwgt || 3 * vk < a.maxvwgt)) return;
   Cand c;
-  c.w = a.adjwgt[j];
+  c.w = w;
   c.k = k;
   c.h = a.mode == CM_MATCH_HEM_HASH ? edge_hash((unsigned)min(v, k), (unsigned)max(v, k)) : 0u;
   if (better(c, best)) best = c;
 }
 
-// Warp-wide best of per-lane candidates (all lanes participate).
-__device__ __forceinline__ int warp_best(const Cand &c) {
+// Per-lane best over entries [b, e) (e - b <= kChunk) of v's row; all loads
+// of the chunk are issued before any is used.
+__device__ __forceinline__ Cand lane_scan(const MatchArgs &a, int v, long long vw, int b, int e) {
+  const int lane = threadIdx.x & 31;
+  constexpr int U = kChunk / 32;
+  int k[U], w[U], s[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int j = b + lane + 32 * u;
+    k[u] = j < e ? a.adjncy[j] : -1;
+    w[u] = j < e ? a.adjwgt[j] : 0;
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) s[u] = k[u] >= 0 ? __ldcg(a.m2 + k[u]) : 0;
+  Cand c{0, 0u, INT_MAX};
+#pragma unroll
+  for (int u = 0; u < U; ++u)
+    if (k[u] >= 0) eval(a, v, vw, k[u], w[u], s[u], c);
+  return c;
+}
+
+__device__ __forceinline__ Cand warp_best(const Cand &c) {
   const unsigned full = 0xffffffffu;
   const bool valid = c.k != INT_MAX;
   const int wmax = __reduce_max_sync(full, valid ? c.w : INT_MIN);
@@ -86,23 +114,90 @@ __device__ __forceinline__ int warp_best(const Cand &c) {
   const unsigned hmin = __reduce_min_sync(full, atw ? c.h : 0xffffffffu);
   const bool ath = atw && c.h == hmin;
   const unsigned kmin = __reduce_min_sync(full, ath ? (unsigned)c.k : 0xffffffffu);
-  return kmin == 0xffffffffu ? -1 : (int)kmin;
+  Cand r;
+  r.w = wmax;
+  r.h = hmin;
+  r.k = kmin == 0xffffffffu ? INT_MAX : (int)kmin;
+  return r;
 }
 
-__device__ __forceinline__ void push_next(const MatchArgs &a, int round, bool want, int x) {
-  // Warp-aggregated, deduplicated by stamp; called convergently by all lanes.
-  bool push = false;
-  if (want) push = atomicMax(a.stamp + x, round + 1) < round + 1;
-  const unsigned mask = __ballot_sync(0xffffffffu, push);
-  if (!mask) return;
+__device__ __forceinline__ unsigned long long warp_excl_scan_u64(unsigned long long v, unsigned long long *total) {
+  const unsigned long long inc = warp_inclusive_scan_u64(v);
+  *total = __shfl_sync(0xffffffffu, inc, 31);
+  return inc - v;
+}
+
+// Adds vertex x (row of `deg` entries) to slot S's work; all lanes call it
+// convergently (warp-aggregated counters).
+__device__ __forceinline__ void append_work(const MatchArgs &a, int par, bool take, int x, int deg) {
+  const Slot &S = a.slot[par];
   const int lane = threadIdx.x & 31;
-  int base = 0;
-  if (lane == __ffs(mask) - 1) base = atomicAdd(a.ctr + ((round + 1) & 1), __popc(mask));
-  base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
-  if (push) a.fr[(round + 1) & 1][base + __popc(mask & ((1u << lane) - 1))] = x;
+  const bool sm = take && deg <= kSerialDeg;
+  const unsigned mask = __ballot_sync(0xffffffffu, sm);
+  if (mask) {
+    const int leader = __ffs(mask) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(a.nsmall + par, __popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (sm) S.small[base + __popc(mask & ((1u << lane) - 1))] = x;
+  }
+  const bool bg = take && deg > kSerialDeg;
+  if (__any_sync(0xffffffffu, bg)) {
+    const int nch = bg ? (deg + kChunk - 1) / kChunk : 0;
+    const unsigned long long mine = bg ? ((1ull << 32) | (unsigned long long)nch) : 0ull;
+    unsigned long long tot;
+    const unsigned long long ex = warp_excl_scan_u64(mine, &tot);
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(a.big + par, tot);
+    base = __shfl_sync(0xffffffffu, base, 0) + ex;
+    if (bg) {
+      const int idx = (int)(base >> 32), cb = (int)(base & 0xffffffffu);
+      S.big_v[idx] = x;
+      S.big_base[idx] = cb;
+      S.big_done[idx] = 0;
+      for (int j = 0; j < nch; ++j) S.big_map[cb + j] = idx;
+    }
+  }
 }
 
-__global__ void __launch_bounds__(kMatchThreads) k_match(MatchArgs a) {
+// Queues x's row as wake chunks for the pair (v, p); convergent call.
+__device__ __forceinline__ void append_wake(const MatchArgs &a, bool take, int x, int deg, int v, int p) {
+  const int lane = threadIdx.x & 31;
+  const bool t = take && deg > 0;
+  if (!__any_sync(0xffffffffu, t)) return;
+  const int nch = t ? (deg + kChunk - 1) / kChunk : 0;
+  const unsigned long long mine = t ? ((1ull << 32) | (unsigned long long)nch) : 0ull;
+  unsigned long long tot;
+  const unsigned long long ex = warp_excl_scan_u64(mine, &tot);
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(a.wk, tot);
+  base = __shfl_sync(0xffffffffu, base, 0) + ex;
+  if (t) {
+    const int idx = (int)(base >> 32), cb = (int)(base & 0xffffffffu);
+    a.wk_x[idx] = x;
+    a.wk_v[idx] = v;
+    a.wk_p[idx] = p;
+    a.wk_base[idx] = cb;
+    for (int j = 0; j < nch; ++j) a.wk_map[cb + j] = idx;
+  }
+}
+
+__device__ __forceinline__ bool wakes(const MatchArgs &a, int x, int v, int p) {
+  if (x == v || x == p) return false;
+  const int px = __ldcg(a.ptr + x);
+  return (px == v || px == p) && __ldcg(a.m2 + x) < 0;
+}
+
+// Puts x into round nr's work unless already there (stamp); convergent.
+__device__ __forceinline__ void push_next(const MatchArgs &a, int nr, bool want, int x) {
+  bool push = false;
+  if (want) push = atomicMax(a.stamp + x, nr) < nr;
+  int deg = 0;
+  if (push) deg = a.xadj[x + 1] - a.xadj[x];
+  append_work(a, nr & 1, push, x, deg);
+}
+
+__global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
   const int lane = threadIdx.x & 31;
   const long long gthread = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nthreads = (long long)gridDim.x * blockDim.x;
@@ -111,70 +206,113 @@ __global__ void __launch_bounds__(kMatchThreads) k_match(MatchArgs a) {
   const int n = a.n;
   DevStatus *st = a.st;
 
+  if (gthread == 0) {
+    a.nsmall[0] = a.nsmall[1] = 0;
+    a.big[0] = a.big[1] = 0;
+    a.wk[0] = 0;
+  }
   for (long long v = gthread; v < n; v += nthreads) {
     a.m2[v] = -1 - a.vwgt[v];
     a.ptr[v] = -1;
     a.stamp[v] = 0;
   }
-  if (gthread == 0) { a.ctr[0] = 0; a.ctr[1] = 0; }
+  if (!grid_barrier(st, gridDim.x)) return;
+  // round 0 works on every vertex that has a neighbour
+  for (long long b0 = (long long)gwarp * 32; b0 < n; b0 += (long long)nwarps * 32) {
+    const long long v = b0 + lane;
+    const int deg = v < n ? a.xadj[v + 1] - a.xadj[v] : 0;
+    append_work(a, 0, deg > 0, (int)v, deg);
+  }
   if (!grid_barrier(st, gridDim.x)) return;
 
   int round = 0;
   for (;; ++round) {
-    const int count = round == 0 ? n : __ldcg(a.ctr + (round & 1));
-    if (count == 0) break;
+    const int par = round & 1;
+    const Slot &S = a.slot[par];
+    const int nsmall = __ldcg(a.nsmall + par);
+    const unsigned long long bc = __ldcg(a.big + par);
+    const int nbig = (int)(bc >> 32), nchunks = (int)(bc & 0xffffffffu);
+    if (nsmall == 0 && nbig == 0) break;
     if (round >= a.max_rounds) {
       if (gthread == 0) record_error(st, CM_ERR_LIMIT, ERR_SITE_ROUNDS);
       break;
     }
-    const int *front = a.fr[round & 1];
-    if (gthread == 0) a.ctr[(round + 1) & 1] = 0;
+    if (gthread == 0) {  // next round's slot and this round's wake list start empty
+      a.nsmall[par ^ 1] = 0;
+      a.big[par ^ 1] = 0;
+      a.wk[0] = 0;
+    }
 
-    // ---- phase A: recompute candidates --------------------------------
-    for (long long base = (long long)gwarp * 32; base < count; base += (long long)nwarps * 32) {
-      const long long i = base + lane;
-      int v = -1, xs = 0, deg = 0;
-      if (i < count) {
-        v = round == 0 ? (int)i : __ldcg(front + i);
-        if (__ldcg(a.m2 + v) < 0) {
-          xs = a.xadj[v];
-          deg = a.xadj[v + 1] - xs;
-        } else {
-          v = -1;
-        }
-      }
-      const long long vw = v >= 0 ? -1ll - __ldcg(a.m2 + v) : 0;
+    // ---- phase A: candidates ----------------------------------------------
+    for (long long b0 = (long long)gwarp * 32; b0 < nsmall; b0 += (long long)nwarps * 32) {
+      const long long i = b0 + lane;
+      if (i >= nsmall) continue;
+      const int v = __ldcg(S.small + i);
+      const int sv = __ldcg(a.m2 + v);
+      if (sv >= 0) continue;
+      const long long vw = -1ll - sv;
+      const int xs = a.xadj[v], deg = a.xadj[v + 1] - xs;
+      int k[kSerialDeg], s[kSerialDeg];
+#pragma unroll
+      for (int t = 0; t < kSerialDeg; ++t) k[t] = t < deg ? a.adjncy[xs + t] : -1;
+#pragma unroll
+      for (int t = 0; t < kSerialDeg; ++t) s[t] = k[t] >= 0 ? __ldcg(a.m2 + k[t]) : 0;
       Cand best{0, 0u, INT_MAX};
-      const bool serial = v >= 0 && deg <= kSerialDeg;
-      if (serial) {
-        for (int j = xs; j < xs + deg; ++j) consider(a, v, vw, j, best);
-        a.ptr[v] = best.k == INT_MAX ? -1 : best.k;
+#pragma unroll
+      for (int t = 0; t < kSerialDeg; ++t)
+        if (k[t] >= 0 && s[t] < 0) eval(a, v, vw, k[t], a.adjwgt[xs + t], s[t], best);
+      a.ptr[v] = best.k == INT_MAX ? -1 : best.k;
+    }
+    for (int q = gwarp; q < nchunks; q += nwarps) {
+      const int i = __ldcg(S.big_map + q);
+      const int v = __ldcg(S.big_v + i);
+      const int sv = __ldcg(a.m2 + v);
+      if (sv >= 0) continue;  // matched: nothing to recompute (uniform per warp)
+      const int xs = a.xadj[v], xe = a.xadj[v + 1];
+      const int nch = (xe - xs + kChunk - 1) / kChunk;
+      const int j = q - __ldcg(S.big_base + i);
+      const int b = xs + j * kChunk, e = min(xe, b + kChunk);
+      const Cand r = warp_best(lane_scan(a, v, -1ll - sv, b, e));
+      if (nch == 1) {
+        if (lane == 0) a.ptr[v] = r.k == INT_MAX ? -1 : r.k;
+        continue;
       }
-      unsigned longs = __ballot_sync(0xffffffffu, v >= 0 && !serial);
-      while (longs) {
-        const int src = __ffs(longs) - 1;
-        longs &= longs - 1;
-        const int vv = __shfl_sync(0xffffffffu, v, src);
-        const int xx = __shfl_sync(0xffffffffu, xs, src);
-        const int dd = __shfl_sync(0xffffffffu, deg, src);
-        const long long ww = __shfl_sync(0xffffffffu, vw, src);
-        Cand c{0, 0u, INT_MAX};
-        for (int j = xx + lane; j < xx + dd; j += 32) consider(a, vv, ww, j, c);
-        const int b = warp_best(c);
-        if (lane == 0) a.ptr[vv] = b;
+      int last = 0;
+      if (lane == 0) {
+        a.part_w[q] = r.w;
+        a.part_h[q] = r.h;
+        a.part_k[q] = r.k;
+        __threadfence();
+        last = atomicAdd(S.big_done + i, 1) == nch - 1;
+      }
+      last = __shfl_sync(0xffffffffu, last, 0);
+      if (last) {  // reduce this row's chunk bests
+        __threadfence();
+        const int base = __ldcg(S.big_base + i);
+        Cand cc{0, 0u, INT_MAX};
+        for (int t = lane; t < nch; t += 32) {
+          Cand o;
+          o.k = __ldcg(a.part_k + base + t);
+          o.w = __ldcg(a.part_w + base + t);
+          o.h = __ldcg(a.part_h + base + t);
+          if (better(o, cc)) cc = o;
+        }
+        const Cand rr = warp_best(cc);
+        if (lane == 0) a.ptr[v] = rr.k == INT_MAX ? -1 : rr.k;
       }
     }
     if (!grid_barrier(st, gridDim.x)) return;
 
-    // ---- phase B: commit mutual pairs, wake waiting neighbours ---------
-    for (long long base = (long long)gwarp * 32; base < count; base += (long long)nwarps * 32) {
-      const long long i = base + lane;
+    // ---- phase B: commit mutual pairs --------------------------------------
+    const long long total = (long long)nsmall + nbig;
+    for (long long b0 = (long long)gwarp * 32; b0 < total; b0 += (long long)nwarps * 32) {
+      const long long i = b0 + lane;
       int v = -1, p = -1;
-      if (i < count) {
-        v = round == 0 ? (int)i : __ldcg(front + i);
+      if (i < total) {
+        v = i < nsmall ? __ldcg(S.small + i) : __ldcg(S.big_v + (i - nsmall));
         p = __ldcg(a.ptr + v);
         bool commit = p >= 0 && __ldcg(a.m2 + v) < 0 && __ldcg(a.ptr + p) == v;
-        // Both ends in this frontier: the lower id commits.
+        // Both ends in this round's work: the lower id commits.
         if (commit && p < v && __ldcg(a.stamp + p) == round) commit = false;
         if (commit) {
           a.m2[v] = p;
@@ -183,47 +321,49 @@ __global__ void __launch_bounds__(kMatchThreads) k_match(MatchArgs a) {
           v = -1;
         }
       }
-      // Wake neighbours x of v and p with ptr[x] in {v, p}.
       int xv = 0, dv = 0, xp = 0, dp = 0;
       if (v >= 0) {
         xv = a.xadj[v]; dv = a.xadj[v + 1] - xv;
         xp = a.xadj[p]; dp = a.xadj[p + 1] - xp;
       }
       const bool serial = v >= 0 && dv + dp <= kSerialDeg;
+      // long pairs: queue both rows as wake chunks for phase C
+      append_wake(a, v >= 0 && !serial, v, dv, v, p);
+      append_wake(a, v >= 0 && !serial, p, dp, v, p);
       const int smax = __reduce_max_sync(0xffffffffu, serial ? dv + dp : 0);
       for (int t = 0; t < smax; ++t) {
         bool want = false;
         int x = 0;
         if (serial && t < dv + dp) {
           x = t < dv ? a.adjncy[xv + t] : a.adjncy[xp + t - dv];
-          if (x != v && x != p) {
-            const int px = __ldcg(a.ptr + x);
-            want = (px == v || px == p) && __ldcg(a.m2 + x) < 0;
-          }
+          want = wakes(a, x, v, p);
         }
-        push_next(a, round, want, x);
+        push_next(a, round + 1, want, x);
       }
-      unsigned longs = __ballot_sync(0xffffffffu, v >= 0 && !serial);
-      while (longs) {
-        const int src = __ffs(longs) - 1;
-        longs &= longs - 1;
-        const int vv = __shfl_sync(0xffffffffu, v, src), pp = __shfl_sync(0xffffffffu, p, src);
-        const int x0 = __shfl_sync(0xffffffffu, xv, src), d0 = __shfl_sync(0xffffffffu, dv, src);
-        const int x1 = __shfl_sync(0xffffffffu, xp, src), d1 = __shfl_sync(0xffffffffu, dp, src);
-        for (int t0 = 0; t0 < d0 + d1; t0 += 32) {
-          const int t = t0 + lane;
-          bool want = false;
-          int x = 0;
-          if (t < d0 + d1) {
-            x = t < d0 ? a.adjncy[x0 + t] : a.adjncy[x1 + t - d0];
-            if (x != vv && x != pp) {
-              const int px = __ldcg(a.ptr + x);
-              want = (px == vv || px == pp) && __ldcg(a.m2 + x) < 0;
-            }
-          }
-          push_next(a, round, want, x);
-        }
+    }
+    if (!grid_barrier(st, gridDim.x)) return;
+
+    // ---- phase C: wake chunks ----------------------------------------------
+    const unsigned long long wc = __ldcg(a.wk);
+    const int wchunks = (int)(wc & 0xffffffffu);
+    for (int q = gwarp; q < wchunks; q += nwarps) {
+      const int i = __ldcg(a.wk_map + q);
+      const int x = __ldcg(a.wk_x + i), v = __ldcg(a.wk_v + i), p = __ldcg(a.wk_p + i);
+      const int j = q - __ldcg(a.wk_base + i);
+      const int xs = a.xadj[x], xe = a.xadj[x + 1];
+      const int b = xs + j * kChunk, e = min(xe, b + kChunk);
+      constexpr int U = kChunk / 32;
+      int y[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int t = b + lane + 32 * u;
+        y[u] = t < e ? a.adjncy[t] : -1;
       }
+      bool want[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) want[u] = y[u] >= 0 && wakes(a, y[u], v, p);
+#pragma unroll
+      for (int u = 0; u < U; ++u) push_next(a, round + 1, want[u], y[u] >= 0 ? y[u] : 0);
     }
     if (!grid_barrier(st, gridDim.x)) return;
   }
@@ -232,34 +372,65 @@ __global__ void __launch_bounds__(kMatchThreads) k_match(MatchArgs a) {
   if (gthread == 0) st->rounds = round;
 }
 
+int64_t max_chunks(int64_t n, int64_t m) { return m / kChunk + n + 64; }
+
 }  // namespace
 
-size_t match_ws_bytes(int64_t n, int64_t) { return (size_t)n * 4 * 4 + 1024; }
+size_t match_ws_bytes(int64_t n, int64_t m) {
+  const int64_t ch = max_chunks(n, m);
+  size_t b = (size_t)n * 4 * 3;                               // ptr, stamp (+slack)
+  b += 2 * ((size_t)n * 4 * 4 + (size_t)ch * 4);              // two slots
+  b += (size_t)n * 4 * 4 + (size_t)ch * 4;                    // wake items + map
+  b += (size_t)ch * 4 * 3;                                    // partials
+  return b + 64 * 256;
+}
 
 int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, int32_t *d_match, cudaStream_t s) {
   const int n = g->nvtxs;
   if (n == 0) return CM_OK;
   if (mode != CM_MATCH_HEM && mode != CM_MATCH_HEM_HASH)
     return cm_fail(CM_ERR_UNSUPPORTED, "cm_match: mode %d not available", mode);
+  const int64_t ch = max_chunks(n, g->nedges);
   MatchArgs a;
   a.n = n;
   a.xadj = g->xadj; a.adjncy = g->adjncy; a.adjwgt = g->adjwgt; a.vwgt = g->vwgt;
   a.maxvwgt = maxvwgt;
   a.mode = mode;
   a.m2 = d_match;
-  a.ptr = (int *)ws_take(ctx, (size_t)n * 4);
-  a.stamp = (int *)ws_take(ctx, (size_t)n * 4);
-  a.fr[0] = (int *)ws_take(ctx, (size_t)n * 4);
-  a.fr[1] = (int *)ws_take(ctx, (size_t)n * 4);
-  a.ctr = (int *)ws_take(ctx, 64);
-  if (!a.ptr || !a.stamp || !a.fr[0] || !a.fr[1] || !a.ctr) return cm_fail(CM_ERR_NOMEM, "cm_match: workspace too small");
-  a.max_rounds = n / 2 + 4;
+  bool ok = true;
+  auto take = [&](size_t bytes) {
+    void *p = ws_take(ctx, bytes);
+    ok = ok && p != nullptr;
+    return (int *)p;
+  };
+  a.ptr = take((size_t)n * 4);
+  a.stamp = take((size_t)n * 4);
+  for (int p = 0; p < 2; ++p) {
+    Slot &S = a.slot[p];
+    S.small = take((size_t)n * 4);
+    S.big_v = take((size_t)n * 4);
+    S.big_base = take((size_t)n * 4);
+    S.big_done = take((size_t)n * 4);
+    S.big_map = take((size_t)ch * 4);
+  }
+  a.wk_x = take((size_t)n * 4);
+  a.wk_v = take((size_t)n * 4);
+  a.wk_p = take((size_t)n * 4);
+  a.wk_base = take((size_t)n * 4);
+  a.wk_map = take((size_t)ch * 4);
+  a.part_w = take((size_t)ch * 4);
+  a.part_k = take((size_t)ch * 4);
+  a.part_h = (unsigned *)take((size_t)ch * 4);
+  a.nsmall = take(64);
+  a.big = (unsigned long long *)take(64);
+  a.wk = (unsigned long long *)take(64);
+  if (!ok) return cm_fail(CM_ERR_NOMEM, "cm_match: workspace too small");
+  a.max_rounds = n + 8;
   a.st = ctx->d_status;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_match, kMatchThreads, 0);
-  if (per_sm < 1) per_sm = 1;
-  long long want = ((long long)n + kMatchThreads - 1) / kMatchThreads;
-  int grid = (int)std::min<long long>((long long)ctx->num_sms * per_sm, std::max<long long>(1, want));
+  if (per_sm < 1) return cm_fail(CM_ERR_CUDA, "cm_match: kernel cannot be resident");
+  const int grid = ctx->num_sms * per_sm;
   void *args[] = {(void *)&a};
   stage_begin(ctx, s);
   cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_match, dim3(grid), dim3(kMatchThreads), args, 0, s);
