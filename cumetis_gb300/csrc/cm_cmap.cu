@@ -160,3 +160,78 @@ int launch_cmap(cm_ctx *ctx, int32_t n, const int32_t *xadj, const int32_t *vwgt
 }
 
 }  // namespace cm
+
+// ---------------------------------------------------------------------------
+// cm_build_cmap_noalloc: the same coarse-vertex map for callers that must not
+// allocate device memory after start-up -- hosts whose memory planner owns
+// every device allocation, or latency-critical loops that cannot absorb the
+// device-wide synchronisation a cudaMalloc may cause.  Its only scratch (the
+// look-back status words and a status block) is the file-scope array below,
+// which every GPU that loads this library holds until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace cm {
+namespace {
+
+constexpr int kNoAllocMaxVertices = 1 << 24;                     // 16,777,216
+constexpr int kNoAllocTiles = kNoAllocMaxVertices / kCmapTile;   // 8,192
+constexpr int kNoAllocStatusWords = (int)((sizeof(DevStatus) + 7) / 8);
+constexpr int kNoAllocWords = kNoAllocStatusWords + kNoAllocTiles + 2;  // 65,584 bytes
+
+// [status block][look-back ticket][one status word per tile]
+static __device__ __align__(256) unsigned long long g_cmap_noalloc_scratch[kNoAllocWords];
+
+// In host code the array's name is only a stand-in; the device address comes
+// from cudaGetSymbolAddress, looked up once per device with that device
+// current.
+constexpr int kNoAllocMaxDevices = 64;
+struct NoAllocDevice {
+  std::once_flag once;
+  cudaError_t err = cudaSuccess;
+  unsigned long long *scratch = nullptr;
+  int num_sms = 0;
+};
+NoAllocDevice g_noalloc_devices[kNoAllocMaxDevices];
+
+}  // namespace
+}  // namespace cm
+
+extern "C" int cm_build_cmap_noalloc(int32_t nvtxs, const int32_t *d_xadj, const int32_t *d_vwgt,
+                                     const int32_t *d_match, int32_t *d_cmap, int32_t *d_leader,
+                                     int32_t *d_cvwgt, int32_t *d_eoff, int32_t *d_cnvtxs, void *stream) {
+  using namespace cm;
+  if (nvtxs < 0 || (nvtxs > 0 && (!d_xadj || !d_vwgt || !d_match || !d_cmap || !d_leader || !d_cvwgt)) ||
+      !d_eoff || !d_cnvtxs)
+    return cm_fail(CM_ERR_INVALID, "cm_build_cmap_noalloc: bad arguments");
+  if (nvtxs > kNoAllocMaxVertices)
+    return cm_fail(CM_ERR_INVALID,
+                   "cm_build_cmap_noalloc: %d vertices exceed its fixed scratch (at most %d); use cm_build_cmap",
+                   nvtxs, kNoAllocMaxVertices);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_status(e, "cm_build_cmap_noalloc: cudaGetDevice");
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return cm_fail(CM_ERR_UNSUPPORTED, "cm_build_cmap_noalloc: device %d", dev);
+  NoAllocDevice &D = g_noalloc_devices[dev];
+  std::call_once(D.once, [&D, dev]() {
+    D.err = cudaGetSymbolAddress((void **)&D.scratch, g_cmap_noalloc_scratch);
+    if (D.err == cudaSuccess) D.err = cudaDeviceGetAttribute(&D.num_sms, cudaDevAttrMultiProcessorCount, dev);
+  });
+  if (D.err != cudaSuccess || !D.scratch) return cuda_status(D.err, "cm_build_cmap_noalloc: scratch set-up");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (nvtxs == 0) {
+    cudaMemsetAsync(d_cnvtxs, 0, sizeof(int32_t), s);
+    cudaMemsetAsync(d_eoff, 0, sizeof(int32_t), s);
+    return cuda_status(cudaGetLastError(), "cm_build_cmap_noalloc(empty)");
+  }
+  DevStatus *st = reinterpret_cast<DevStatus *>(D.scratch);
+  unsigned long long *lb = D.scratch + kNoAllocStatusWords;
+  const int ntiles = (nvtxs + kCmapTile - 1) / kCmapTile;
+  // The array keeps the previous call's contents: clear the status block, the
+  // ticket and this call's tile words.
+  cudaMemsetAsync(D.scratch, 0, (size_t)(kNoAllocStatusWords + ntiles + 1) * 8, s);
+  k_cmap<<<ntiles, kCmapThreads, 0, s>>>(nvtxs, d_xadj, d_vwgt, d_match, d_cmap, d_leader, d_cvwgt, d_eoff, d_cnvtxs,
+                                          nullptr, INT32_MAX, nullptr, 1, nullptr, nullptr, 1, lb, st);
+  k_cmap_followers<<<D.num_sms * 8, 256, 0, s>>>(nvtxs, d_match, d_cmap, st);
+  return cuda_status(cudaGetLastError(), "cm_build_cmap_noalloc launch");
+}

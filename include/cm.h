@@ -153,6 +153,24 @@ int cm_build_cmap(cm_ctx *ctx, int32_t nvtxs, const int32_t *d_xadj, const int32
                   const int32_t *d_match, int32_t *d_cmap, int32_t *d_leader,
                   int32_t *d_cvwgt, int32_t *d_eoff, int32_t *d_cnvtxs, void *stream);
 
+/* cm_build_cmap without any device allocation.  No counterpart in the
+ * reference: it exists for callers that must not allocate device memory after
+ * start-up (a host whose memory planner owns every device allocation, or a
+ * latency-critical loop that cannot absorb the device-wide synchronisation a
+ * cudaMalloc may cause).  Same arguments and outputs as cm_build_cmap, minus
+ * the context; runs on the current device.  Its scratch is a fixed 64 KB
+ * array inside the library, held by every GPU that loads it until exit, so
+ * nvtxs is limited to 16,777,216 (larger inputs: CM_ERR_INVALID).  The first
+ * call on a device looks up that array's device address; make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU (other streams, other threads) race and must be serialised by the
+ * caller.  Problems the kernels detect (an out-of-range or non-involutive
+ * matching, a look-back wait past its time limit) are recorded in the array
+ * and not reported; pass only valid matchings, or use cm_build_cmap. */
+int cm_build_cmap_noalloc(int32_t nvtxs, const int32_t *d_xadj, const int32_t *d_vwgt,
+                          const int32_t *d_match, int32_t *d_cmap, int32_t *d_leader,
+                          int32_t *d_cvwgt, int32_t *d_eoff, int32_t *d_cnvtxs, void *stream);
+
 /* Contraction given a matching (replaces cuMetis_gpu_create_cgraph,
  * cuMetis.cu:1291-1406, with its bb_segsort and Sort_cnedges2_part1..3).
  * Output contract: coarse vertex c <-> leader c in increasing leader order;
