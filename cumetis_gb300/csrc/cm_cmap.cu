@@ -27,6 +27,7 @@ k_cmap(int n, const int *__restrict__ xadj, const int *__restrict__ vwgt, const 
        int *__restrict__ cmap, int *__restrict__ leader, int *__restrict__ cvwgt, int *__restrict__ eoff,
        int *__restrict__ d_cnvtxs, int *__restrict__ long_list, int long_thr, unsigned long long *long_ctr,
        int long_chunk, int *__restrict__ chunk_row, int *__restrict__ first_row, int tile_diag,
+       int *__restrict__ mid_list, int *__restrict__ mid_ctr, int mid_cap,
        unsigned long long *__restrict__ lb, DevStatus *st) {
   __shared__ int s_tile;
   __shared__ unsigned long long s_warp[kCmapThreads / 32];
@@ -95,13 +96,19 @@ k_cmap(int n, const int *__restrict__ xadj, const int *__restrict__ vwgt, const 
         if (c == 0) first_row[0] = 0;
       }
       if (L > long_thr) {
-        const int nch = (L + long_chunk - 1) / long_chunk;
-        unsigned long long old = atomicAdd(long_ctr, (1ull << 32) | (unsigned long long)nch);
-        const int idx = (int)(old >> 32);
-        const int cbase = (int)(old & 0xffffffffu);
-        long_list[2 * idx] = c;
-        long_list[2 * idx + 1] = cbase;  // first chunk index of this row
-        for (int j = 0; j < nch; ++j) chunk_row[cbase + j] = idx;
+        if (L > long_chunk) {  // sorted in chunks and merged
+          const int nch = (L + long_chunk - 1) / long_chunk;
+          unsigned long long old = atomicAdd(long_ctr, (1ull << 32) | (unsigned long long)nch);
+          const int idx = (int)(old >> 32);
+          const int cbase = (int)(old & 0xffffffffu);
+          long_list[2 * idx] = c;
+          long_list[2 * idx + 1] = cbase;  // first chunk index of this row
+          for (int j = 0; j < nch; ++j) chunk_row[cbase + j] = idx;
+        } else {  // sorted whole by one block of the row's size class
+          const int cls = L <= 2 * long_thr ? 0 : (L <= 4 * long_thr ? 1 : 2);
+          const int idx = atomicAdd(mid_ctr + cls, 1);
+          mid_list[(size_t)cls * mid_cap + idx] = c;
+        }
       }
       row_max = L > row_max ? L : row_max;
     }
@@ -136,7 +143,8 @@ size_t cmap_ws_bytes(int64_t n) { return (size_t)((n + kCmapTile - 1) / kCmapTil
 int launch_cmap(cm_ctx *ctx, int32_t n, const int32_t *xadj, const int32_t *vwgt, const int32_t *match,
                 int32_t *cmap, int32_t *leader, int32_t *cvwgt, int32_t *eoff, int32_t *d_cnvtxs,
                 int32_t *long_list, int32_t long_threshold, int32_t long_chunk, unsigned long long *d_long_ctr,
-                int32_t *chunk_row, int32_t *first_row, int32_t tile_diag, cudaStream_t s) {
+                int32_t *chunk_row, int32_t *first_row, int32_t tile_diag, int32_t *mid_list, int32_t *mid_ctr,
+                int32_t mid_cap, cudaStream_t s) {
   if (n == 0) {
     cudaMemsetAsync(d_cnvtxs, 0, sizeof(int32_t), s);
     cudaMemsetAsync(eoff, 0, sizeof(int32_t), s);
@@ -150,7 +158,8 @@ int launch_cmap(cm_ctx *ctx, int32_t n, const int32_t *xadj, const int32_t *vwgt
   k_cmap<<<ntiles, kCmapThreads, 0, s>>>(n, xadj, vwgt, match, cmap, leader, cvwgt, eoff, d_cnvtxs, long_list,
                                           long_list ? long_threshold : INT32_MAX, d_long_ctr,
                                           long_chunk > 0 ? long_chunk : 1, chunk_row, first_row,
-                                          tile_diag > 0 ? tile_diag : 1, lb, ctx->d_status);
+                                          tile_diag > 0 ? tile_diag : 1, mid_list, mid_ctr, mid_cap, lb,
+                                          ctx->d_status);
   ctx->launches++;
   int blocks = ctx->num_sms * 8;
   k_cmap_followers<<<blocks, 256, 0, s>>>(n, match, cmap, ctx->d_status);
@@ -231,7 +240,8 @@ extern "C" int cm_build_cmap_noalloc(int32_t nvtxs, const int32_t *d_xadj, const
   // ticket and this call's tile words.
   cudaMemsetAsync(D.scratch, 0, (size_t)(kNoAllocStatusWords + ntiles + 1) * 8, s);
   k_cmap<<<ntiles, kCmapThreads, 0, s>>>(nvtxs, d_xadj, d_vwgt, d_match, d_cmap, d_leader, d_cvwgt, d_eoff, d_cnvtxs,
-                                          nullptr, INT32_MAX, nullptr, 1, nullptr, nullptr, 1, lb, st);
+                                          nullptr, INT32_MAX, nullptr, 1, nullptr, nullptr, 1, nullptr, nullptr, 0, lb,
+                                          st);
   k_cmap_followers<<<D.num_sms * 8, 256, 0, s>>>(nvtxs, d_match, d_cmap, st);
   return cuda_status(cudaGetLastError(), "cm_build_cmap_noalloc launch");
 }

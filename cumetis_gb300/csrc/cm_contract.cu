@@ -31,13 +31,13 @@
 namespace cm {
 namespace {
 
-constexpr int kTileThreads = 256;
-constexpr int kTileE = 8;
+constexpr int kTileThreads = 128;
+constexpr int kTileE = 4;
 constexpr int kTileDiag = 512;                    // D
-constexpr int kLongThr = 2048;                    // rows longer than this take the long path
+constexpr int kLongThr = 1024;                    // rows longer than this take the long path
 constexpr int kTileCap = kTileDiag + kLongThr;    // max entries in a tile (multiple of kTileE)
 constexpr int kChunk = 8192;                      // long-row chunk (entries sorted per block)
-constexpr int kChunkThreads = 512;
+constexpr int kChunkThreads = 1024;
 constexpr unsigned kSelfKey = 0xffffffffu;        // self loops sort last in their row
 
 // Composite sort key (tile-local row, coarse id).  32-bit when coarse ids fit
@@ -95,7 +95,7 @@ __device__ __forceinline__ int upper_bound_smem(const int *a, int n, int x) {
 __device__ __forceinline__ int expanded_src(int o, int xl, int dl, int xf) { return o < dl ? xl + o : xf + (o - dl); }
 
 template <typename K>
-__global__ void __launch_bounds__(kTileThreads, sizeof(K) == 4 ? 4 : 2)
+__global__ void __launch_bounds__(kTileThreads, sizeof(K) == 4 ? 6 : 3)
 k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
                  const int *__restrict__ match, const int *__restrict__ cmap, const int *__restrict__ leader,
                  const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
@@ -104,6 +104,11 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
   using KT = KeyT<K>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TileSmem<K> &S = *reinterpret_cast<TileSmem<K> *>(smem_raw);
+  // 32-bit keys: (k0, w0) and (k1, w1) are used as packed 64-bit words
+  // (key << 32 | weight), sorted as one array each.
+  constexpr bool kPacked = sizeof(K) == 4;
+  unsigned long long *P0 = reinterpret_cast<unsigned long long *>(S.k0);
+  unsigned long long *P1 = reinterpret_cast<unsigned long long *>(S.k1);
   const int tid = threadIdx.x;
   const int nc = *d_cn;
   const long long m = eoff[nc];
@@ -189,8 +194,12 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
       const int e = e0 + u * kTileThreads;
       if (e < ntot) {
         const unsigned id = (x[u] == clo + rr[u]) ? KT::kSelf : (unsigned)x[u];
-        S.k0[e] = KT::make(rr[u], id);
-        S.w0[e] = w[u];
+        if constexpr (kPacked) {
+          P0[e] = ((unsigned long long)KT::make(rr[u], id) << 32) | (unsigned)w[u];
+        } else {
+          S.k0[e] = KT::make(rr[u], id);
+          S.w0[e] = w[u];
+        }
       }
     }
   }
@@ -198,8 +207,9 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
   // tile's aggregate is published before the (longer) sort: later tiles never
   // wait on this tile's sort in their look-back.
   constexpr int kHash = (int)((sizeof(K) + 4) * kTileCap / sizeof(K));
+  const unsigned hsize = (unsigned)min(kHash, 2 * ntot + 1);  // load factor <= 1/2 (2/3 for 64-bit keys)
   K *tab = S.k1;
-  for (int i = tid; i < kHash; i += kTileThreads) tab[i] = KT::kPad;
+  for (int i = tid; i < (int)hsize; i += kTileThreads) tab[i] = KT::kPad;
   int long_sum = 0;
 #pragma unroll
   for (int i = 0; i < kRowsPerThread; ++i) {
@@ -209,23 +219,28 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
   __syncthreads();
   int uniq = long_sum;
   for (int e = tid; e < ntot; e += kTileThreads) {
-    const K key = S.k0[e];
+    const K key = kPacked ? (K)(P0[e] >> 32) : S.k0[e];
     if (KT::id(key) == KT::kSelf) continue;
-    unsigned h = (unsigned)(((unsigned long long)key * 0x9E3779B97F4A7C15ull) >> 32) % (unsigned)kHash;
-    for (int probe = 0; probe < kHash; ++probe) {
+    unsigned h = (unsigned)(((unsigned long long)key * 0x9E3779B97F4A7C15ull) >> 32) % hsize;
+    for (unsigned probe = 0; probe < hsize; ++probe) {
       const K old = atomicCAS(&tab[h], KT::kPad, key);
       if (old == KT::kPad) { ++uniq; break; }
       if (old == key) break;
-      h = h + 1 == (unsigned)kHash ? 0u : h + 1;
+      h = h + 1 == hsize ? 0u : h + 1;
     }
   }
   int agg;
   block_exclusive_scan<kTileThreads>(uniq, S.scan, &agg);
   if (tid < 32) lookback_publish(lb, tile, (unsigned long long)agg);
   __syncthreads();
-  const int b = block_merge_sort<K, kTileThreads, kTileE>(S.k0, S.w0, S.k1, S.w1, ntot, KT::kPad);
-  const K *Ks = b ? S.k1 : S.k0;
-  const int *W = b ? S.w1 : S.w0;
+  int b;
+  if constexpr (kPacked) b = block_merge_sort_packed<kTileThreads, kTileE>(P0, P1, ntot);
+  else b = block_merge_sort<K, kTileThreads, kTileE>(S.k0, S.w0, S.k1, S.w1, ntot, KT::kPad);
+  const unsigned long long *Ps = b ? P1 : P0;
+  const K *Kw = b ? S.k1 : S.k0;
+  const int *Ww = b ? S.w1 : S.w0;
+  auto keyat = [&](int i) -> K { if constexpr (kPacked) return (K)(Ps[i] >> 32); else return Kw[i]; };
+  auto wat = [&](int i) -> int { if constexpr (kPacked) return (int)(unsigned)Ps[i]; else return Ww[i]; };
   int *hs = reinterpret_cast<int *>(b ? S.k0 : S.k1);  // exclusive head count, ntot + 1 ints
 
   // Heads (first of a run of equal (row, id), not a self loop): one block scan
@@ -234,15 +249,15 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
   const int i0 = min(ntot, tid * ipt), i1 = min(ntot, i0 + ipt);
   int hcnt = 0;
   for (int i = i0; i < i1; ++i) {
-    const K k = Ks[i];
-    hcnt += (KT::id(k) != KT::kSelf) && (i == 0 || Ks[i - 1] != k);
+    const K k = keyat(i);
+    hcnt += (KT::id(k) != KT::kSelf) && (i == 0 || keyat(i - 1) != k);
   }
   int htot;
   int run = block_exclusive_scan<kTileThreads>(hcnt, S.scan, &htot);
   for (int i = i0; i < i1; ++i) {
-    const K k = Ks[i];
+    const K k = keyat(i);
     hs[i] = run;
-    run += (KT::id(k) != KT::kSelf) && (i == 0 || Ks[i - 1] != k);
+    run += (KT::id(k) != KT::kSelf) && (i == 0 || keyat(i - 1) != k);
   }
   if (tid == 0) hs[ntot] = htot;
   __syncthreads();
@@ -285,10 +300,10 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
   for (int i = tid; i < ntot; i += kTileThreads) {
     const int hb = hs[i];
     if (hs[i + 1] == hb) continue;  // not a head
-    const K k = Ks[i];
+    const K k = keyat(i);
     const int r = KT::row(k);
-    unsigned sum = (unsigned)W[i];
-    for (int j = i + 1; j < ntot && Ks[j] == k; ++j) sum += (unsigned)W[j];
+    unsigned sum = (unsigned)wat(i);
+    for (int j = i + 1; j < ntot && keyat(j) == k; ++j) sum += (unsigned)wat(j);
     const long long pos = base + S.r_c[r] + (hb - hs[S.r_start[r]]);
     cadjncy[pos] = (int)KT::id(k);
     cadjwgt[pos] = (int)sum;
@@ -302,10 +317,11 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
 // ---------------------------------------------------------------------------
 // Long rows
 // ---------------------------------------------------------------------------
-struct ChunkSmem {
-  unsigned k[2][kChunk];
-  int w[2][kChunk];
+template <int CAP>
+struct RowSmem {
+  unsigned long long v[2][CAP + 8];  // packed (coarse id << 32 | weight); +8 for the sentinel hs[cnt]
 };
+using ChunkSmem = RowSmem<kChunk>;
 
 __device__ __forceinline__ void long_row_info(const int *long_list, int idx, const int *leader, const int *match,
                                               const int *xadj, const int *eoff, int &c, int &L, int &xl, int &dl,
@@ -327,6 +343,102 @@ __host__ __device__ __forceinline__ int merge_passes(int L) {
   return p;
 }
 
+// Gathers entries [cs, cs+cnt) of coarse row c's expanded row into shared
+// memory and sorts them.  If `whole` (the segment is the entire row), merges
+// duplicates and writes the unique entries to dedup_dst and their count to
+// *ucount_c; otherwise writes the sorted run to run_dst.
+template <int NT, int CAP>
+__device__ __forceinline__ void sort_row_segment(RowSmem<CAP> &S, int *scan, int c, int xl, int dl, int xf, int cs,
+                                                 int cnt, bool whole, int2 *run_dst, int2 *dedup_dst, int *ucount_c,
+                                                 const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
+                                                 const int *__restrict__ cmap) {
+  for (int t0 = threadIdx.x; t0 < cnt; t0 += 4 * NT) {
+    int src[4], x[4], w[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int t = t0 + u * NT;
+      src[u] = t < cnt ? expanded_src(cs + t, xl, dl, xf) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      x[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
+      w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int t = t0 + u * NT;
+      if (t < cnt) {
+        const unsigned key = x[u] == c ? kSelfKey : (unsigned)x[u];
+        S.v[0][t] = ((unsigned long long)key << 32) | (unsigned)w[u];
+      }
+    }
+  }
+  __syncthreads();
+  const int b = block_merge_sort_packed<NT, 8>(S.v[0], S.v[1], cnt);
+  const unsigned long long *P = S.v[b];
+  if (!whole) {
+    for (int t = threadIdx.x; t < cnt; t += NT) {
+      const unsigned long long e = P[t];
+      run_dst[t] = make_int2((int)(unsigned)(e >> 32), (int)(unsigned)e);
+    }
+  } else {
+    int *hs = reinterpret_cast<int *>(S.v[b ^ 1]);
+    const int ipt = (cnt + NT - 1) / NT;
+    const int i0 = min(cnt, (int)threadIdx.x * ipt), i1 = min(cnt, i0 + ipt);
+    auto head = [&](int i) {
+      const unsigned k = (unsigned)(P[i] >> 32);
+      return k != kSelfKey && (i == 0 || (unsigned)(P[i - 1] >> 32) != k);
+    };
+    int hc = 0;
+    for (int i = i0; i < i1; ++i) hc += head(i);
+    int tot;
+    int run = block_exclusive_scan<NT>(hc, scan, &tot);
+    for (int i = i0; i < i1; ++i) {
+      hs[i] = run;
+      run += head(i);
+    }
+    if (threadIdx.x == 0) { hs[cnt] = tot; *ucount_c = tot; }
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += NT) {
+      if (hs[i + 1] == hs[i]) continue;
+      const unsigned k = (unsigned)(P[i] >> 32);
+      unsigned sum = (unsigned)P[i];
+      for (int j = i + 1; j < cnt && (unsigned)(P[j] >> 32) == k; ++j) sum += (unsigned)P[j];
+      dedup_dst[hs[i]] = make_int2((int)k, (int)sum);
+    }
+  }
+  __syncthreads();
+}
+
+// Rows too long for a tile but <= kChunk entries, one size class per launch:
+// one block sorts and deduplicates one whole row (unique entries to stage1).
+template <int NT, int CAP>
+__global__ void __launch_bounds__(NT)
+k_mid_sort(const int *__restrict__ xadj, const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
+           const int *__restrict__ match, const int *__restrict__ cmap, const int *__restrict__ leader,
+           const int *__restrict__ eoff, const int *__restrict__ list, const int *__restrict__ count,
+           int2 *__restrict__ stage1, int *__restrict__ ucount) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  RowSmem<CAP> &S = *reinterpret_cast<RowSmem<CAP> *>(smem_raw);
+  __shared__ int scan[NT / 32 + 1];
+  const int nrows = *count;
+  for (int i = blockIdx.x; i < nrows; i += gridDim.x) {
+    const int c = list[i];
+    const int l = leader[c];
+    const int f = match[l];
+    const int L = eoff[c + 1] - eoff[c];
+    const int xl = xadj[l];
+    const int dl = xadj[l + 1] - xl;
+    const int xf = f != l ? xadj[f] : 0;
+    sort_row_segment<NT, CAP>(S, scan, c, xl, dl, xf, 0, L, true, nullptr, stage1 + eoff[c], ucount + c, adjncy,
+                              adjwgt, cmap);
+  }
+}
+
+// Rows longer than kChunk: each kChunk-entry chunk sorted into stage0 as one
+// run for the merge passes.
 __global__ void __launch_bounds__(kChunkThreads, 1)
 k_long_sort(const int *__restrict__ xadj, const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
             const int *__restrict__ match, const int *__restrict__ cmap, const int *__restrict__ leader,
@@ -334,6 +446,7 @@ k_long_sort(const int *__restrict__ xadj, const int *__restrict__ adjncy, const 
             const unsigned long long *long_ctr, int2 *__restrict__ stage) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem &S = *reinterpret_cast<ChunkSmem *>(smem_raw);
+  __shared__ int scan[kChunkThreads / 32 + 1];
   const unsigned long long ctr = *long_ctr;
   const int nchunks = (int)(ctr & 0xffffffffu);
   for (int q = blockIdx.x; q < nchunks; q += gridDim.x) {
@@ -343,34 +456,8 @@ k_long_sort(const int *__restrict__ xadj, const int *__restrict__ adjncy, const 
     const int j = q - long_list[2 * idx + 1];
     const int cs = j * kChunk;
     const int cnt = min(kChunk, L - cs);
-    for (int t0 = threadIdx.x; t0 < cnt; t0 += 4 * kChunkThreads) {
-      int src[4], x[4], w[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int t = t0 + u * kChunkThreads;
-        src[u] = t < cnt ? expanded_src(cs + t, xl, dl, xf) : -1;
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        x[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
-        w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : 0;
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int t = t0 + u * kChunkThreads;
-        if (t < cnt) {
-          S.k[0][t] = x[u] == c ? kSelfKey : (unsigned)x[u];
-          S.w[0][t] = w[u];
-        }
-      }
-    }
-    __syncthreads();
-    const int b = block_merge_sort<unsigned, kChunkThreads, 8>(S.k[0], S.w[0], S.k[1], S.w[1], cnt, kSelfKey);
-    int2 *dst = stage + eoff[c] + cs;
-    for (int t = threadIdx.x; t < cnt; t += kChunkThreads) dst[t] = make_int2((int)S.k[b][t], S.w[b][t]);
-    __syncthreads();
+    sort_row_segment<kChunkThreads, kChunk>(S, scan, c, xl, dl, xf, cs, cnt, false, stage + eoff[c] + cs, nullptr,
+                                            nullptr, adjncy, adjwgt, cmap);
   }
 }
 
@@ -443,19 +530,21 @@ k_long_merge(const int *__restrict__ long_list, const int *__restrict__ chunk_ro
 
 // Deduplicates each long row (sorted, in stage[merge_passes(L) & 1]) into the
 // other stage, compacted at eoff[c]; ucount[c] = unique entries.
-__global__ void __launch_bounds__(kTileThreads)
+constexpr int kDedupThreads = 512;
+__global__ void __launch_bounds__(kDedupThreads)
 k_long_dedup(const int *__restrict__ long_list, const int *__restrict__ eoff, const unsigned long long *long_ctr,
              int2 *stage0, int2 *stage1, int *__restrict__ ucount) {
-  __shared__ int scan[kTileThreads / 32 + 1];
+  __shared__ int scan[kDedupThreads / 32 + 1];
   const int nlong = (int)(*long_ctr >> 32);
   for (int idx = blockIdx.x; idx < nlong; idx += gridDim.x) {
     const int c = long_list[2 * idx];
     const int L = eoff[c + 1] - eoff[c];
+    if (L <= kChunk) continue;  // (not in this list)
     const int fb = merge_passes(L) & 1;
     const int2 *src = (fb ? stage1 : stage0) + eoff[c];
     int2 *dst = (fb ? stage0 : stage1) + eoff[c];
     int carry = 0;
-    for (int b = 0; b < L; b += kTileThreads) {
+    for (int b = 0; b < L; b += kDedupThreads) {
       const int i = b + threadIdx.x;
       int h = 0;
       int2 e = make_int2(0, 0);
@@ -464,7 +553,7 @@ k_long_dedup(const int *__restrict__ long_list, const int *__restrict__ eoff, co
         h = ((unsigned)e.x != kSelfKey) && (i == 0 || src[i - 1].x != e.x);
       }
       int tot;
-      const int ex = block_exclusive_scan<kTileThreads>(h, scan, &tot);
+      const int ex = block_exclusive_scan<kDedupThreads>(h, scan, &tot);
       if (h) {
         unsigned sum = (unsigned)e.y;
         for (int j = i + 1; j < L && src[j].x == e.x; ++j) sum += (unsigned)src[j].y;
@@ -476,22 +565,38 @@ k_long_dedup(const int *__restrict__ long_list, const int *__restrict__ eoff, co
   }
 }
 
+// Copies every long row's unique entries to its final place once the tiles
+// have fixed cxadj: first the size-class rows (stage1), then the chunked rows.
 __global__ void k_long_copy(const int *__restrict__ long_list, const int *__restrict__ chunk_row,
                             const int *__restrict__ eoff, const unsigned long long *long_ctr,
+                            const int *__restrict__ mid_list, const int *__restrict__ mid_ctr, int mid_cap,
                             const int2 *stage0, const int2 *stage1, const int *__restrict__ ucount,
                             const int *__restrict__ cxadj, int *__restrict__ cadjncy, int *__restrict__ cadjwgt) {
+  const int n0 = mid_ctr[0], n1 = mid_ctr[1], n2 = mid_ctr[2];
+  const int nmid = n0 + n1 + n2;
   const int nchunks = (int)(*long_ctr & 0xffffffffu);
-  for (int q = blockIdx.x; q < nchunks; q += gridDim.x) {
-    const int idx = chunk_row[q];
-    const int c = long_list[2 * idx];
-    const int L = eoff[c + 1] - eoff[c];
-    const int fb = merge_passes(L) & 1;
-    const int2 *src = (fb ? stage0 : stage1) + eoff[c];
-    const int j = q - long_list[2 * idx + 1];
-    const int cnt = ucount[c];
+  for (int q = blockIdx.x; q < nmid + nchunks; q += gridDim.x) {
+    int c, lo, hi;
+    const int2 *src;
+    if (q < nmid) {
+      const int cls = q < n0 ? 0 : (q < n0 + n1 ? 1 : 2);
+      const int i = q - (cls == 0 ? 0 : (cls == 1 ? n0 : n0 + n1));
+      c = mid_list[(size_t)cls * mid_cap + i];
+      src = stage1 + eoff[c];
+      lo = 0;
+      hi = ucount[c];
+    } else {
+      const int qq = q - nmid;
+      const int idx = chunk_row[qq];
+      c = long_list[2 * idx];
+      const int L = eoff[c + 1] - eoff[c];
+      src = ((merge_passes(L) & 1) ? stage0 : stage1) + eoff[c];
+      const int j = qq - long_list[2 * idx + 1];
+      lo = j * kChunk;
+      hi = min(ucount[c], (j + 1) * kChunk);
+    }
     const long long dst = cxadj[c];
-    const int hi = min(cnt, (j + 1) * kChunk);
-    for (int t = j * kChunk + threadIdx.x; t < hi; t += blockDim.x) {
+    for (int t = lo + threadIdx.x; t < hi; t += blockDim.x) {
       const int2 e = src[t];
       cadjncy[dst + t] = e.x;
       cadjwgt[dst + t] = e.y;
@@ -507,7 +612,8 @@ size_t contract_ws_bytes(int64_t n, int64_t m) {
   size_t b = 0;
   b += (size_t)n * 4 * 3 + 4 * 256;          // leader, ucount, eoff(+1)
   b += (size_t)(ntiles + 2) * 4 + 256;       // first_row
-  b += (size_t)(m / kLongThr + 2) * 8 + 256; // long_list
+  b += (size_t)(m / kChunk + 2) * 8 + 256;   // long_list
+  b += (size_t)(m / (kLongThr + 1) + 2) * 12 + 256;  // size-class lists
   b += (size_t)nchunks * 4 + 256;            // chunk_row
   b += 256;                                  // counters
   b += (size_t)(ntiles + 2) * 8 + 256;       // tile look-back
@@ -526,45 +632,69 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   }
   const int64_t ntiles = (n + m) / kTileDiag + 1;
   const int64_t nchunks_max = m / kChunk + m / kLongThr + 2;
+  const int64_t mid_cap = m / (kLongThr + 1) + 2;
   int *leader = (int *)ws_take(ctx, (size_t)n * 4);
   int *ucount = (int *)ws_take(ctx, (size_t)n * 4);
   int *eoff = (int *)ws_take(ctx, (size_t)(n + 1) * 4);
   int *first_row = (int *)ws_take(ctx, (size_t)(ntiles + 2) * 4);
-  int *long_list = (int *)ws_take(ctx, (size_t)(m / kLongThr + 2) * 8);
+  int *long_list = (int *)ws_take(ctx, (size_t)(m / kChunk + 2) * 8);
   int *chunk_row = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
-  unsigned long long *ctr = (unsigned long long *)ws_take(ctx, 64);
+  int *mid_list = (int *)ws_take(ctx, (size_t)mid_cap * 3 * 4);
+  unsigned long long *ctr = (unsigned long long *)ws_take(ctx, 64);   // [0] chunked rows, [1] mid counters
   unsigned long long *lb = (unsigned long long *)ws_take(ctx, (size_t)(ntiles + 2) * 8);
   int2 *stage0 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
   int2 *stage1 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
-  if (!leader || !ucount || !eoff || !first_row || !long_list || !chunk_row || !ctr || !lb || !stage0 || !stage1)
+  if (!leader || !ucount || !eoff || !first_row || !long_list || !chunk_row || !mid_list || !ctr || !lb || !stage0 ||
+      !stage1)
     return cm_fail(CM_ERR_NOMEM, "contract: workspace too small");
+  int *mid_ctr = reinterpret_cast<int *>(ctr + 1);
   DevStatus *st = ctx->d_status;
   cudaMemsetAsync(ctr, 0, 64, s);
   cudaMemsetAsync(&st->max_row, 0, sizeof(int), s);
   cudaMemsetAsync(lb, 0, (size_t)(ntiles + 1) * 8, s);
   int rc = launch_cmap(ctx, (int32_t)n, fine->xadj, fine->vwgt, match, cmap, leader, coarse->vwgt, eoff,
                        d_sizes /* n' lands in d_sizes[0] */, long_list, kLongThr, kChunk, ctr, chunk_row, first_row,
-                       kTileDiag, s);
+                       kTileDiag, mid_list, mid_ctr, (int32_t)mid_cap, s);
   if (rc) return rc;
-  const int persistent = ctx->num_sms;
+  const int sms = ctx->num_sms;
   const bool small_ids = n < kSmallIdLimit;
   const size_t tile_smem = small_ids ? sizeof(TileSmem<unsigned>) : sizeof(TileSmem<unsigned long long>);
-  const size_t chunk_smem = sizeof(ChunkSmem);
   if (small_ids)
     cudaFuncSetAttribute(k_contract_tiles<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem);
   else
     cudaFuncSetAttribute(k_contract_tiles<unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)tile_smem);
-  cudaFuncSetAttribute(k_long_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)chunk_smem);
+  cudaFuncSetAttribute(k_mid_sort<256, 2 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(RowSmem<2 * kLongThr>));
+  cudaFuncSetAttribute(k_mid_sort<512, 4 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(RowSmem<4 * kLongThr>));
+  cudaFuncSetAttribute(k_mid_sort<1024, kChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(RowSmem<kChunk>));
+  cudaFuncSetAttribute(k_long_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem));
+
+  // Long rows: the three size classes run on the auxiliary streams while the
+  // chunked rows are sorted, merged and deduplicated on the caller's stream;
+  // the tiles wait for all of them (they need every long row's unique count).
   stage_begin(ctx, s);
-  k_long_sort<<<persistent, kChunkThreads, chunk_smem, s>>>(fine->xadj, fine->adjncy, fine->adjwgt, match, cmap,
-                                                             leader, eoff, long_list, chunk_row, ctr, stage0);
-  stage_end(ctx, CM_STAGE_LONG_SORT, s);
+  cudaEventRecord(ctx->fork_ev, s);
+  for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(ctx->aux[i], ctx->fork_ev, 0);
+  k_mid_sort<256, 2 * kLongThr><<<sms * 4, 256, sizeof(RowSmem<2 * kLongThr>), ctx->aux[0]>>>(
+      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, mid_list, mid_ctr + 0, stage1, ucount);
+  k_mid_sort<512, 4 * kLongThr><<<sms * 2, 512, sizeof(RowSmem<4 * kLongThr>), ctx->aux[1]>>>(
+      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, mid_list + mid_cap, mid_ctr + 1, stage1,
+      ucount);
+  k_mid_sort<1024, kChunk><<<sms, 1024, sizeof(RowSmem<kChunk>), ctx->aux[2]>>>(
+      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, mid_list + 2 * mid_cap, mid_ctr + 2, stage1,
+      ucount);
+  ctx->launches += 3;
+  for (int i = 0; i < 3; ++i) cudaEventRecord(ctx->join_ev[i], ctx->aux[i]);
+  k_long_sort<<<sms, kChunkThreads, sizeof(ChunkSmem), s>>>(fine->xadj, fine->adjncy, fine->adjwgt, match, cmap,
+                                                           leader, eoff, long_list, chunk_row, ctr, stage0);
   ctx->launches++;
   {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_long_merge, kMergeThreads, 0);
-    int grid = ctx->num_sms * (per_sm > 0 ? per_sm : 1);
+    int grid = sms * (per_sm > 0 ? per_sm : 1);
     const int *a0 = long_list;
     const int *a1 = chunk_row;
     const int *a2 = eoff;
@@ -572,17 +702,16 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
     int2 *a4 = stage0, *a5 = stage1;
     DevStatus *a6 = st;
     void *args[] = {(void *)&a0, (void *)&a1, (void *)&a2, (void *)&a3, (void *)&a4, (void *)&a5, (void *)&a6};
-    stage_begin(ctx, s);
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_long_merge, dim3(grid), dim3(kMergeThreads), args, 0, s);
-    stage_end(ctx, CM_STAGE_LONG_MERGE, s);
     if (e != cudaSuccess) return cuda_status(e, "contract: long-row merge launch");
     ctx->launches++;
   }
-  stage_begin(ctx, s);
-  k_long_dedup<<<persistent * 4, kTileThreads, 0, s>>>(long_list, eoff, ctr, stage0, stage1, ucount);
-  stage_end(ctx, CM_STAGE_LONG_DEDUP, s);
+  k_long_dedup<<<sms * 2, kDedupThreads, 0, s>>>(long_list, eoff, ctr, stage0, stage1, ucount);
   ctx->launches++;
-  // d_sizes[0] temporarily holds n' (written by the cmap scan).
+  for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(s, ctx->join_ev[i], 0);
+  stage_end(ctx, CM_STAGE_LONG_SORT, s);
+
+  // d_sizes[0] holds n' (written by the cmap scan).
   stage_begin(ctx, s);
   if (small_ids)
     k_contract_tiles<unsigned><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
@@ -595,8 +724,8 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   stage_end(ctx, CM_STAGE_TILES, s);
   ctx->launches++;
   stage_begin(ctx, s);
-  k_long_copy<<<persistent * 4, 256, 0, s>>>(long_list, chunk_row, eoff, ctr, stage0, stage1, ucount, coarse->xadj,
-                                              coarse->adjncy, coarse->adjwgt);
+  k_long_copy<<<sms * 4, 256, 0, s>>>(long_list, chunk_row, eoff, ctr, mid_list, mid_ctr, (int)mid_cap, stage0,
+                                       stage1, ucount, coarse->xadj, coarse->adjncy, coarse->adjwgt);
   stage_end(ctx, CM_STAGE_LONG_COPY, s);
   ctx->launches++;
   return check_launch(ctx, "contract");

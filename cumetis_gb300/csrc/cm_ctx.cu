@@ -161,6 +161,11 @@ extern "C" int cm_ctx_create(int device, cm_ctx **out) {
   if (!rc) rc = cuda_status(cudaMemset(ctx->d_status, 0, sizeof(DevStatus)), "status init");
   if (!rc) rc = cuda_status(cudaMallocHost(&ctx->h_status, sizeof(DevStatus)), "pinned status alloc");
   if (!rc) rc = cuda_status(cudaMallocHost(&ctx->h_small, 64), "pinned readback alloc");
+  for (int i = 0; i < 3 && !rc; ++i) {
+    rc = cuda_status(cudaStreamCreateWithFlags(&ctx->aux[i], cudaStreamNonBlocking), "aux stream");
+    if (!rc) rc = cuda_status(cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming), "aux event");
+  }
+  if (!rc) rc = cuda_status(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming), "fork event");
   if (!rc) {
     // Keep freed level buffers in the stream-ordered pool between calls.
     cudaMemPool_t pool;
@@ -187,6 +192,12 @@ extern "C" void cm_ctx_destroy(cm_ctx *ctx) {
   if (ctx->d_status) cudaFree(ctx->d_status);
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   if (ctx->h_small) cudaFreeHost(ctx->h_small);
+  if (ctx->d_trace) cudaFree(ctx->d_trace);
+  for (int i = 0; i < 3; ++i) {
+    if (ctx->aux[i]) cudaStreamDestroy(ctx->aux[i]);
+    if (ctx->join_ev[i]) cudaEventDestroy(ctx->join_ev[i]);
+  }
+  if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
   delete ctx;
 }
 
@@ -212,6 +223,37 @@ extern "C" int cm_ctx_stage_times(cm_ctx *ctx, double *ms, int32_t cap, int rese
   for (int i = 0; i < cap && i < CM_STAGE_COUNT; ++i) ms[i] = ctx->stage_ms[i];
   if (reset)
     for (double &v : ctx->stage_ms) v = 0.0;
+  return CM_OK;
+}
+
+extern "C" int cm_ctx_set_match_trace(cm_ctx *ctx, int32_t max_rounds) {
+  if (!ctx || max_rounds < 0) return cm_fail(CM_ERR_INVALID, "cm_ctx_set_match_trace: bad arguments");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  if (ctx->d_trace) {
+    cudaDeviceSynchronize();
+    cudaFree(ctx->d_trace);
+    ctx->d_trace = nullptr;
+    ctx->trace_rows = 0;
+  }
+  if (max_rounds == 0) return CM_OK;
+  const size_t bytes = (size_t)(max_rounds + 1) * 8 * sizeof(unsigned long long);
+  if ((rc = cuda_status(cudaMalloc(&ctx->d_trace, bytes), "trace alloc"))) return rc;
+  cudaMemset(ctx->d_trace, 0, bytes);
+  ctx->trace_rows = max_rounds + 1;
+  return CM_OK;
+}
+
+extern "C" int cm_ctx_match_trace(cm_ctx *ctx, int64_t *out, int32_t cap_rows, int32_t *rows_out) {
+  if (!ctx || !out || cap_rows < 1) return cm_fail(CM_ERR_INVALID, "cm_ctx_match_trace: bad arguments");
+  if (!ctx->d_trace) return cm_fail(CM_ERR_INVALID, "cm_ctx_match_trace: tracing is off");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  const int rows = std::min(cap_rows, ctx->trace_rows);
+  if ((rc = cuda_status(cudaDeviceSynchronize(), "trace sync"))) return rc;
+  if ((rc = cuda_status(cudaMemcpy(out, ctx->d_trace, (size_t)rows * 64, cudaMemcpyDeviceToHost), "trace copy")))
+    return rc;
+  if (rows_out) *rows_out = std::min<int64_t>(rows, out[4] + 2);
   return CM_OK;
 }
 
@@ -258,7 +300,7 @@ extern "C" int cm_build_cmap(cm_ctx *ctx, int32_t nvtxs, const int32_t *d_xadj, 
   ws_reset(ctx);
   if ((rc = ws_ensure(ctx, cmap_ws_bytes(nvtxs)))) return rc;
   return launch_cmap(ctx, nvtxs, d_xadj, d_vwgt, d_match, d_cmap, d_leader, d_cvwgt, d_eoff, d_cnvtxs, nullptr, 0,
-                     1, nullptr, nullptr, nullptr, 0, (cudaStream_t)stream);
+                     1, nullptr, nullptr, nullptr, 0, nullptr, nullptr, 0, (cudaStream_t)stream);
 }
 
 extern "C" int cm_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *d_match, int32_t *d_cmap,

@@ -27,6 +27,12 @@ struct cm_ctx {
   std::vector<Pending> pending;
   double stage_ms[CM_STAGE_COUNT] = {0};
   cudaEvent_t ev_open = nullptr;
+  // internal streams/events for concurrent contraction stages
+  cudaStream_t aux[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t fork_ev = nullptr, join_ev[3] = {nullptr, nullptr, nullptr};
+  // matching trace (optional): 8 x uint64 per row, row 0 = header
+  unsigned long long *d_trace = nullptr;
+  int trace_rows = 0;
 };
 
 namespace cm {
@@ -58,7 +64,8 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
 int launch_cmap(cm_ctx *ctx, int32_t n, const int32_t *xadj, const int32_t *vwgt, const int32_t *match,
                 int32_t *cmap, int32_t *leader, int32_t *cvwgt, int32_t *eoff, int32_t *d_cnvtxs,
                 int32_t *long_list, int32_t long_threshold, int32_t long_chunk, unsigned long long *d_long_ctr,
-                int32_t *chunk_row, int32_t *first_row, int32_t tile_diag, cudaStream_t s);
+                int32_t *chunk_row, int32_t *first_row, int32_t tile_diag, int32_t *mid_list, int32_t *mid_ctr,
+                int32_t mid_cap, cudaStream_t s);
 int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int32_t *cmap, cm_graph *coarse,
                     int32_t *d_sizes, cudaStream_t s);
 

@@ -13,16 +13,18 @@
 // that order whatever the schedule.
 //
 // One persistent cooperative kernel (one 1024-thread block per SM) runs all
-// rounds.  A round has three phases separated by grid barriers:
-//   A  (m2[] frozen)  every vertex of the round's work recomputes ptr[v], its
-//      best candidate.  Rows of <= kSerialDeg entries: one lane each.  Longer
-//      rows: kChunk-entry chunks, one warp each (edge-balanced across the
-//      grid); the last chunk of a row to finish reduces the chunk bests.
-//   B  (ptr[] frozen) mutual pointers commit (m2[v]=p, m2[p]=v).  A pair whose
-//      two rows are short wakes its neighbours x with ptr[x] in the pair at
-//      once; longer pairs queue their rows as wake chunks.
-//   C  wake chunks: neighbours with ptr[x] in the pair join the next round.
-// Vertices whose candidate is still unmatched keep their pointer and wait.
+// rounds; a round has three phases separated by grid barriers:
+//   A  full scans: every vertex in the round's scan list computes its kTop
+//      best eligible unmatched candidates (cached) and points at the first.
+//      Rows of <= kSerialDeg entries: one lane each; longer rows: kChunk-entry
+//      chunks, one warp each, the last chunk of a row merging the chunk lists.
+//   B  commits: a vertex whose pointer changed this round (scanned, or updated
+//      from its cache) and whose target points back forms a pair.
+//   C  filter of the active list (unmatched vertices with a candidate): a
+//      vertex whose target got matched takes the next unmatched entry of its
+//      cached list (candidates only disappear and eligibility is fixed, so the
+//      cached order stays exact); only an exhausted, incomplete cache sends it
+//      back to phase A for a full scan.
 // m2[v] < 0 encodes "unmatched, vwgt = -1 - m2[v]": one 4-byte gather per
 // neighbour answers both "matched?" and the weight cap.
 #include <climits>
@@ -35,11 +37,14 @@ namespace {
 constexpr int kMatchThreads = 1024;
 constexpr int kSerialDeg = 16;   // rows scanned by one lane
 constexpr int kChunk = 256;      // entries per warp work item
+constexpr int kTop = 4;          // cached candidates per vertex
+constexpr int kNotScanned = -2;  // top[v*kTop] before the first scan
 
-struct Slot {      // work of one round (double-buffered by round parity)
-  int *small;      // vertices with rows <= kSerialDeg
-  int *big_v, *big_base, *big_done;  // longer rows, first chunk index, chunks done
-  int *big_map;    // chunk -> index into big_v
+struct Slot {      // lists feeding one round (double-buffered by round parity)
+  int *small;      // full scans, rows <= kSerialDeg
+  int *big_v, *big_base, *big_done, *big_map;   // full scans, longer rows (chunked)
+  int *upd;        // pointers already updated from the cache
+  int *act;        // active list for the round's phase C
 };
 
 struct MatchArgs {
@@ -47,16 +52,15 @@ struct MatchArgs {
   const int *xadj, *adjncy, *adjwgt, *vwgt;
   long long maxvwgt;
   int mode;
-  int *m2, *ptr, *stamp;
+  int *m2, *ptr, *stamp, *top;
   Slot slot[2];
-  int *wk_x, *wk_v, *wk_p, *wk_base, *wk_map;   // wake items of the current round
-  int *nsmall;                   // nsmall[0..1]
-  unsigned long long *big;       // big[0..1] = (rows << 32 | chunks)
-  unsigned long long *wk;        // (items << 32 | chunks)
-  int *part_w, *part_k;          // per chunk partial best
-  unsigned *part_h;
+  int *nsmall, *nupd, *nact;     // [2] each
+  unsigned long long *big;       // [2] = (rows << 32 | chunks)
+  int *part;                     // per chunk: kTop x (w, h, k)
   int max_rounds;
   DevStatus *st;
+  unsigned long long *trace;     // optional: row 0 header, row r+1 = round r
+  int trace_rows;
 };
 
 struct Cand {
@@ -73,37 +77,32 @@ __device__ __forceinline__ bool better(const Cand &a, const Cand &b) {
   return a.k < b.k;
 }
 
-__device__ __forceinline__ void eval(const MatchArgs &a, int v, long long vw, int k, int w, int s, Cand &best) {
-  if (k == v || s >= 0) return;  // self or matched
-  const long long vk = -1ll - s;
-  if (vw + vk > a.maxvwgt) return;
-  if (!(3 * vw < a.maxvwgt || 3 * vk < a.maxvwgt)) return;
-  Cand c;
-  c.w = w;
-  c.k = k;
-  c.h = a.mode == CM_MATCH_HEM_HASH ? edge_hash((unsigned)min(v, k), (unsigned)max(v, k)) : 0u;
-  if (better(c, best)) best = c;
-}
-
-// Per-lane best over entries [b, e) (e - b <= kChunk) of v's row; all loads
-// of the chunk are issued before any is used.
-__device__ __forceinline__ Cand lane_scan(const MatchArgs &a, int v, long long vw, int b, int e) {
-  const int lane = threadIdx.x & 31;
-  constexpr int U = kChunk / 32;
-  int k[U], w[U], s[U];
+// Sorted (best first) list of up to kTop candidates held in registers.
+struct TopK {
+  Cand c[kTop];
+  __device__ __forceinline__ void clear() {
 #pragma unroll
-  for (int u = 0; u < U; ++u) {
-    const int j = b + lane + 32 * u;
-    k[u] = j < e ? a.adjncy[j] : -1;
-    w[u] = j < e ? a.adjwgt[j] : 0;
+    for (int i = 0; i < kTop; ++i) c[i] = Cand{0, 0u, INT_MAX};
   }
+  __device__ __forceinline__ void insert(const Cand &x) {
+    if (!better(x, c[kTop - 1])) return;
+    Cand cur = x;
 #pragma unroll
-  for (int u = 0; u < U; ++u) s[u] = k[u] >= 0 ? __ldcg(a.m2 + k[u]) : 0;
-  Cand c{0, 0u, INT_MAX};
-#pragma unroll
-  for (int u = 0; u < U; ++u)
-    if (k[u] >= 0) eval(a, v, vw, k[u], w[u], s[u], c);
-  return c;
+    for (int i = 0; i < kTop; ++i) {
+      if (better(cur, c[i])) { Cand t = c[i]; c[i] = cur; cur = t; }
+    }
+  }
+};
+
+__device__ __forceinline__ bool eligible_cand(const MatchArgs &a, int v, long long vw, int k, int w, int s, Cand &out) {
+  if (k == v || s >= 0) return false;  // self or matched
+  const long long vk = -1ll - s;
+  if (vw + vk > a.maxvwgt) return false;
+  if (!(3 * vw < a.maxvwgt || 3 * vk < a.maxvwgt)) return false;
+  out.w = w;
+  out.k = k;
+  out.h = a.mode == CM_MATCH_HEM_HASH ? edge_hash((unsigned)min(v, k), (unsigned)max(v, k)) : 0u;
+  return true;
 }
 
 __device__ __forceinline__ Cand warp_best(const Cand &c) {
@@ -121,80 +120,96 @@ __device__ __forceinline__ Cand warp_best(const Cand &c) {
   return r;
 }
 
+// Merges the lanes' sorted lists into the warp's best kTop (all lanes get it).
+__device__ __forceinline__ TopK warp_topk(TopK t) {
+  TopK out;
+  int head = 0;
+#pragma unroll
+  for (int i = 0; i < kTop; ++i) {
+    Cand mine = Cand{0, 0u, INT_MAX};
+#pragma unroll
+    for (int j = 0; j < kTop; ++j)
+      if (j == head) mine = t.c[j];
+    const Cand win = warp_best(mine);
+    out.c[i] = win;
+    if (win.k != INT_MAX && mine.k == win.k && mine.w == win.w && mine.h == win.h) ++head;
+  }
+  return out;
+}
+
+// Per-lane kTop over entries [b, e) (e - b <= kChunk) of v's row; all loads of
+// the chunk are issued before any is used.
+__device__ __forceinline__ TopK lane_scan(const MatchArgs &a, int v, long long vw, int b, int e) {
+  const int lane = threadIdx.x & 31;
+  constexpr int U = kChunk / 32;
+  int k[U], w[U], s[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int j = b + lane + 32 * u;
+    k[u] = j < e ? a.adjncy[j] : -1;
+    w[u] = j < e ? a.adjwgt[j] : 0;
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) s[u] = k[u] >= 0 ? __ldcg(a.m2 + k[u]) : 0;
+  TopK t;
+  t.clear();
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    Cand c;
+    if (k[u] >= 0 && eligible_cand(a, v, vw, k[u], w[u], s[u], c)) t.insert(c);
+  }
+  return t;
+}
+
+__device__ __forceinline__ void store_top(const MatchArgs &a, int v, const TopK &t) {
+  int4 q;
+  q.x = t.c[0].k == INT_MAX ? -1 : t.c[0].k;
+  q.y = t.c[1].k == INT_MAX ? -1 : t.c[1].k;
+  q.z = t.c[2].k == INT_MAX ? -1 : t.c[2].k;
+  q.w = t.c[3].k == INT_MAX ? -1 : t.c[3].k;
+  reinterpret_cast<int4 *>(a.top)[v] = q;
+  a.ptr[v] = q.x;
+}
+
 __device__ __forceinline__ unsigned long long warp_excl_scan_u64(unsigned long long v, unsigned long long *total) {
   const unsigned long long inc = warp_inclusive_scan_u64(v);
   *total = __shfl_sync(0xffffffffu, inc, 31);
   return inc - v;
 }
 
-// Adds vertex x (row of `deg` entries) to slot S's work; all lanes call it
-// convergently (warp-aggregated counters).
-__device__ __forceinline__ void append_work(const MatchArgs &a, int par, bool take, int x, int deg) {
-  const Slot &S = a.slot[par];
+// Warp-aggregated append of x to list[counter]; convergent call.
+__device__ __forceinline__ void warp_append(int *list, int *counter, bool take, int x) {
+  const unsigned mask = __ballot_sync(0xffffffffu, take);
+  if (!mask) return;
   const int lane = threadIdx.x & 31;
-  const bool sm = take && deg <= kSerialDeg;
-  const unsigned mask = __ballot_sync(0xffffffffu, sm);
-  if (mask) {
-    const int leader = __ffs(mask) - 1;
-    int base = 0;
-    if (lane == leader) base = atomicAdd(a.nsmall + par, __popc(mask));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (sm) S.small[base + __popc(mask & ((1u << lane) - 1))] = x;
-  }
-  const bool bg = take && deg > kSerialDeg;
-  if (__any_sync(0xffffffffu, bg)) {
-    const int nch = bg ? (deg + kChunk - 1) / kChunk : 0;
-    const unsigned long long mine = bg ? ((1ull << 32) | (unsigned long long)nch) : 0ull;
-    unsigned long long tot;
-    const unsigned long long ex = warp_excl_scan_u64(mine, &tot);
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(a.big + par, tot);
-    base = __shfl_sync(0xffffffffu, base, 0) + ex;
-    if (bg) {
-      const int idx = (int)(base >> 32), cb = (int)(base & 0xffffffffu);
-      S.big_v[idx] = x;
-      S.big_base[idx] = cb;
-      S.big_done[idx] = 0;
-      for (int j = 0; j < nch; ++j) S.big_map[cb + j] = idx;
-    }
-  }
+  const int leader = __ffs(mask) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(mask));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (take) list[base + __popc(mask & ((1u << lane) - 1))] = x;
 }
 
-// Queues x's row as wake chunks for the pair (v, p); convergent call.
-__device__ __forceinline__ void append_wake(const MatchArgs &a, bool take, int x, int deg, int v, int p) {
+// Queues x (row of `deg` entries) for a full scan in slot `par`; convergent.
+__device__ __forceinline__ void append_scan(const MatchArgs &a, int par, bool take, int x, int deg) {
+  const Slot &S = a.slot[par];
+  warp_append(S.small, a.nsmall + par, take && deg <= kSerialDeg, x);
+  const bool bg = take && deg > kSerialDeg;
+  if (!__any_sync(0xffffffffu, bg)) return;
   const int lane = threadIdx.x & 31;
-  const bool t = take && deg > 0;
-  if (!__any_sync(0xffffffffu, t)) return;
-  const int nch = t ? (deg + kChunk - 1) / kChunk : 0;
-  const unsigned long long mine = t ? ((1ull << 32) | (unsigned long long)nch) : 0ull;
+  const int nch = bg ? (deg + kChunk - 1) / kChunk : 0;
+  const unsigned long long mine = bg ? ((1ull << 32) | (unsigned long long)nch) : 0ull;
   unsigned long long tot;
   const unsigned long long ex = warp_excl_scan_u64(mine, &tot);
   unsigned long long base = 0;
-  if (lane == 0) base = atomicAdd(a.wk, tot);
+  if (lane == 0) base = atomicAdd(a.big + par, tot);
   base = __shfl_sync(0xffffffffu, base, 0) + ex;
-  if (t) {
+  if (bg) {
     const int idx = (int)(base >> 32), cb = (int)(base & 0xffffffffu);
-    a.wk_x[idx] = x;
-    a.wk_v[idx] = v;
-    a.wk_p[idx] = p;
-    a.wk_base[idx] = cb;
-    for (int j = 0; j < nch; ++j) a.wk_map[cb + j] = idx;
+    S.big_v[idx] = x;
+    S.big_base[idx] = cb;
+    S.big_done[idx] = 0;
+    for (int j = 0; j < nch; ++j) S.big_map[cb + j] = idx;
   }
-}
-
-__device__ __forceinline__ bool wakes(const MatchArgs &a, int x, int v, int p) {
-  if (x == v || x == p) return false;
-  const int px = __ldcg(a.ptr + x);
-  return (px == v || px == p) && __ldcg(a.m2 + x) < 0;
-}
-
-// Puts x into round nr's work unless already there (stamp); convergent.
-__device__ __forceinline__ void push_next(const MatchArgs &a, int nr, bool want, int x) {
-  bool push = false;
-  if (want) push = atomicMax(a.stamp + x, nr) < nr;
-  int deg = 0;
-  if (push) deg = a.xadj[x + 1] - a.xadj[x];
-  append_work(a, nr & 1, push, x, deg);
 }
 
 __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
@@ -205,23 +220,29 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
   const int nwarps = (int)(nthreads >> 5);
   const int n = a.n;
   DevStatus *st = a.st;
+  const bool tracer = a.trace != nullptr && gthread == 0;
+  auto trace = [&](int row, int col, unsigned long long v) {
+    if (tracer && row < a.trace_rows) a.trace[row * 8 + col] = v;
+  };
+  trace(0, 0, global_timer_ns());
 
   if (gthread == 0) {
-    a.nsmall[0] = a.nsmall[1] = 0;
+    a.nsmall[0] = a.nsmall[1] = a.nupd[0] = a.nupd[1] = a.nact[0] = a.nact[1] = 0;
     a.big[0] = a.big[1] = 0;
-    a.wk[0] = 0;
   }
   for (long long v = gthread; v < n; v += nthreads) {
     a.m2[v] = -1 - a.vwgt[v];
     a.ptr[v] = -1;
     a.stamp[v] = 0;
+    a.top[v * kTop] = kNotScanned;
   }
   if (!grid_barrier(st, gridDim.x)) return;
-  // round 0 works on every vertex that has a neighbour
+  // Round 0 scans every vertex that has a neighbour: short rows straight from
+  // the vertex range, longer rows through the chunk list built here.
   for (long long b0 = (long long)gwarp * 32; b0 < n; b0 += (long long)nwarps * 32) {
     const long long v = b0 + lane;
     const int deg = v < n ? a.xadj[v + 1] - a.xadj[v] : 0;
-    append_work(a, 0, deg > 0, (int)v, deg);
+    append_scan(a, 0, deg > kSerialDeg, (int)v, deg);
   }
   if (!grid_barrier(st, gridDim.x)) return;
 
@@ -229,147 +250,180 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
   for (;; ++round) {
     const int par = round & 1;
     const Slot &S = a.slot[par];
-    const int nsmall = __ldcg(a.nsmall + par);
+    const Slot &N = a.slot[par ^ 1];
+    // round 0: the short-row scan list and the active list are the vertex range
+    const long long nsmall = round == 0 ? n : __ldcg(a.nsmall + par);
+    const int nupd = __ldcg(a.nupd + par);
+    const long long nact = round == 0 ? n : __ldcg(a.nact + par);
     const unsigned long long bc = __ldcg(a.big + par);
     const int nbig = (int)(bc >> 32), nchunks = (int)(bc & 0xffffffffu);
-    if (nsmall == 0 && nbig == 0) break;
+    if (round == 0) trace(0, 1, global_timer_ns());
+    trace(round + 1, 0, global_timer_ns());
+    trace(round + 1, 4, (unsigned long long)nsmall);
+    trace(round + 1, 5, (unsigned long long)nbig);
+    trace(round + 1, 6, (unsigned long long)nchunks);
+    trace(round + 1, 7, (unsigned long long)nupd);
+    if (nsmall == 0 && nbig == 0 && nupd == 0) break;
     if (round >= a.max_rounds) {
       if (gthread == 0) record_error(st, CM_ERR_LIMIT, ERR_SITE_ROUNDS);
       break;
     }
-    if (gthread == 0) {  // next round's slot and this round's wake list start empty
+    if (gthread == 0) {  // the next round's lists start empty
       a.nsmall[par ^ 1] = 0;
+      a.nupd[par ^ 1] = 0;
+      a.nact[par ^ 1] = 0;
       a.big[par ^ 1] = 0;
-      a.wk[0] = 0;
     }
 
-    // ---- phase A: candidates ----------------------------------------------
+    // ---- phase A: full scans -------------------------------------------------
     for (long long b0 = (long long)gwarp * 32; b0 < nsmall; b0 += (long long)nwarps * 32) {
       const long long i = b0 + lane;
       if (i >= nsmall) continue;
-      const int v = __ldcg(S.small + i);
+      const int v = round == 0 ? (int)i : __ldcg(S.small + i);
+      const int xs = a.xadj[v], deg = a.xadj[v + 1] - xs;
+      if (round == 0 && (deg == 0 || deg > kSerialDeg)) continue;
       const int sv = __ldcg(a.m2 + v);
       if (sv >= 0) continue;
       const long long vw = -1ll - sv;
-      const int xs = a.xadj[v], deg = a.xadj[v + 1] - xs;
       int k[kSerialDeg], s[kSerialDeg];
 #pragma unroll
       for (int t = 0; t < kSerialDeg; ++t) k[t] = t < deg ? a.adjncy[xs + t] : -1;
 #pragma unroll
       for (int t = 0; t < kSerialDeg; ++t) s[t] = k[t] >= 0 ? __ldcg(a.m2 + k[t]) : 0;
-      Cand best{0, 0u, INT_MAX};
+      TopK tk;
+      tk.clear();
 #pragma unroll
-      for (int t = 0; t < kSerialDeg; ++t)
-        if (k[t] >= 0 && s[t] < 0) eval(a, v, vw, k[t], a.adjwgt[xs + t], s[t], best);
-      a.ptr[v] = best.k == INT_MAX ? -1 : best.k;
+      for (int t = 0; t < kSerialDeg; ++t) {
+        Cand c;
+        if (k[t] >= 0 && eligible_cand(a, v, vw, k[t], a.adjwgt[xs + t], s[t], c)) tk.insert(c);
+      }
+      store_top(a, v, tk);
     }
     for (int q = gwarp; q < nchunks; q += nwarps) {
       const int i = __ldcg(S.big_map + q);
       const int v = __ldcg(S.big_v + i);
       const int sv = __ldcg(a.m2 + v);
-      if (sv >= 0) continue;  // matched: nothing to recompute (uniform per warp)
+      if (sv >= 0) continue;  // uniform per warp
       const int xs = a.xadj[v], xe = a.xadj[v + 1];
       const int nch = (xe - xs + kChunk - 1) / kChunk;
       const int j = q - __ldcg(S.big_base + i);
       const int b = xs + j * kChunk, e = min(xe, b + kChunk);
-      const Cand r = warp_best(lane_scan(a, v, -1ll - sv, b, e));
+      const TopK r = warp_topk(lane_scan(a, v, -1ll - sv, b, e));
       if (nch == 1) {
-        if (lane == 0) a.ptr[v] = r.k == INT_MAX ? -1 : r.k;
+        if (lane == 0) store_top(a, v, r);
         continue;
       }
       int last = 0;
+      if (lane < kTop) {
+        Cand mine = r.c[0];
+#pragma unroll
+        for (int t = 1; t < kTop; ++t)
+          if (lane == t) mine = r.c[t];
+        int *p = a.part + ((size_t)q * kTop + lane) * 3;
+        p[0] = mine.w;
+        p[1] = (int)mine.h;
+        p[2] = mine.k;
+      }
       if (lane == 0) {
-        a.part_w[q] = r.w;
-        a.part_h[q] = r.h;
-        a.part_k[q] = r.k;
         __threadfence();
         last = atomicAdd(S.big_done + i, 1) == nch - 1;
       }
       last = __shfl_sync(0xffffffffu, last, 0);
-      if (last) {  // reduce this row's chunk bests
+      if (last) {  // merge the row's chunk lists
         __threadfence();
         const int base = __ldcg(S.big_base + i);
-        Cand cc{0, 0u, INT_MAX};
-        for (int t = lane; t < nch; t += 32) {
+        TopK acc;
+        acc.clear();
+        for (int t = lane; t < nch * kTop; t += 32) {
+          const int *p = a.part + ((size_t)base * kTop + t) * 3;
           Cand o;
-          o.k = __ldcg(a.part_k + base + t);
-          o.w = __ldcg(a.part_w + base + t);
-          o.h = __ldcg(a.part_h + base + t);
-          if (better(o, cc)) cc = o;
+          o.w = __ldcg(p);
+          o.h = (unsigned)__ldcg(p + 1);
+          o.k = __ldcg(p + 2);
+          acc.insert(o);
         }
-        const Cand rr = warp_best(cc);
-        if (lane == 0) a.ptr[v] = rr.k == INT_MAX ? -1 : rr.k;
+        const TopK rr = warp_topk(acc);
+        if (lane == 0) store_top(a, v, rr);
       }
     }
     if (!grid_barrier(st, gridDim.x)) return;
+    trace(round + 1, 1, global_timer_ns());
 
-    // ---- phase B: commit mutual pairs --------------------------------------
-    const long long total = (long long)nsmall + nbig;
-    for (long long b0 = (long long)gwarp * 32; b0 < total; b0 += (long long)nwarps * 32) {
+    // ---- phase B: commit mutual pairs ----------------------------------------
+    // Candidates that changed this round: short scans, chunked scans, cache updates.
+    const long long tot_b = nsmall + nbig + nupd;
+    for (long long i = gthread; i < tot_b; i += nthreads) {
+      int v;
+      if (i < nsmall) {
+        v = round == 0 ? (int)i : __ldcg(S.small + i);
+        if (round == 0) {
+          const int deg = a.xadj[v + 1] - a.xadj[v];
+          if (deg == 0 || deg > kSerialDeg) continue;
+        }
+      } else if (i < nsmall + nbig) {
+        v = __ldcg(S.big_v + (i - nsmall));
+      } else {
+        v = __ldcg(S.upd + (i - nsmall - nbig));
+      }
+      const int p = __ldcg(a.ptr + v);
+      if (p < 0 || __ldcg(a.m2 + v) >= 0 || __ldcg(a.ptr + p) != v) continue;
+      // Both ends changed this round: the lower id commits.
+      if (p < v && __ldcg(a.stamp + p) == round) continue;
+      a.m2[v] = p;
+      a.m2[p] = v;
+    }
+    if (!grid_barrier(st, gridDim.x)) return;
+    trace(round + 1, 2, global_timer_ns());
+
+    // ---- phase C: filter the active list, refresh stale pointers -------------
+    for (long long b0 = (long long)gwarp * 32; b0 < nact; b0 += (long long)nwarps * 32) {
       const long long i = b0 + lane;
-      int v = -1, p = -1;
-      if (i < total) {
-        v = i < nsmall ? __ldcg(S.small + i) : __ldcg(S.big_v + (i - nsmall));
-        p = __ldcg(a.ptr + v);
-        bool commit = p >= 0 && __ldcg(a.m2 + v) < 0 && __ldcg(a.ptr + p) == v;
-        // Both ends in this round's work: the lower id commits.
-        if (commit && p < v && __ldcg(a.stamp + p) == round) commit = false;
-        if (commit) {
-          a.m2[v] = p;
-          a.m2[p] = v;
+      int x = -1;
+      if (i < nact) {
+        x = round == 0 ? (int)i : __ldcg(S.act + i);
+        if (__ldcg(a.m2 + x) >= 0) x = -1;  // matched
+      }
+      const int p = x >= 0 ? __ldcg(a.ptr + x) : -1;
+      if (p < 0) x = -1;                   // no candidate: out for good
+      bool keep = false, upd = false, scan = false;
+      int deg = 0;
+      if (x >= 0) {
+        if (__ldcg(a.m2 + p) < 0) {
+          keep = true;                     // waiting on an unmatched candidate
         } else {
-          v = -1;
+          const int4 c = reinterpret_cast<const int4 *>(a.top)[x];
+          const int cs[kTop] = {c.x, c.y, c.z, c.w};
+          int sm[kTop];
+#pragma unroll
+          for (int t = 0; t < kTop; ++t) sm[t] = cs[t] >= 0 ? __ldcg(a.m2 + cs[t]) : 0;
+          int np = -1;
+#pragma unroll
+          for (int t = kTop - 1; t >= 0; --t)
+            if (cs[t] >= 0 && sm[t] < 0) np = cs[t];
+          if (np >= 0) {
+            a.ptr[x] = np;
+            keep = upd = true;
+          } else if (cs[kTop - 1] < 0) {
+            a.ptr[x] = -1;                 // cache held every candidate: none left
+          } else {
+            keep = scan = true;
+            deg = a.xadj[x + 1] - a.xadj[x];
+          }
         }
       }
-      int xv = 0, dv = 0, xp = 0, dp = 0;
-      if (v >= 0) {
-        xv = a.xadj[v]; dv = a.xadj[v + 1] - xv;
-        xp = a.xadj[p]; dp = a.xadj[p + 1] - xp;
-      }
-      const bool serial = v >= 0 && dv + dp <= kSerialDeg;
-      // long pairs: queue both rows as wake chunks for phase C
-      append_wake(a, v >= 0 && !serial, v, dv, v, p);
-      append_wake(a, v >= 0 && !serial, p, dp, v, p);
-      const int smax = __reduce_max_sync(0xffffffffu, serial ? dv + dp : 0);
-      for (int t = 0; t < smax; ++t) {
-        bool want = false;
-        int x = 0;
-        if (serial && t < dv + dp) {
-          x = t < dv ? a.adjncy[xv + t] : a.adjncy[xp + t - dv];
-          want = wakes(a, x, v, p);
-        }
-        push_next(a, round + 1, want, x);
-      }
+      if (upd || scan) atomicMax(a.stamp + x, round + 1);
+      warp_append(N.act, a.nact + (par ^ 1), keep, x);
+      warp_append(N.upd, a.nupd + (par ^ 1), upd, x);
+      append_scan(a, par ^ 1, scan, x, deg);
     }
     if (!grid_barrier(st, gridDim.x)) return;
-
-    // ---- phase C: wake chunks ----------------------------------------------
-    const unsigned long long wc = __ldcg(a.wk);
-    const int wchunks = (int)(wc & 0xffffffffu);
-    for (int q = gwarp; q < wchunks; q += nwarps) {
-      const int i = __ldcg(a.wk_map + q);
-      const int x = __ldcg(a.wk_x + i), v = __ldcg(a.wk_v + i), p = __ldcg(a.wk_p + i);
-      const int j = q - __ldcg(a.wk_base + i);
-      const int xs = a.xadj[x], xe = a.xadj[x + 1];
-      const int b = xs + j * kChunk, e = min(xe, b + kChunk);
-      constexpr int U = kChunk / 32;
-      int y[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int t = b + lane + 32 * u;
-        y[u] = t < e ? a.adjncy[t] : -1;
-      }
-      bool want[U];
-#pragma unroll
-      for (int u = 0; u < U; ++u) want[u] = y[u] >= 0 && wakes(a, y[u], v, p);
-#pragma unroll
-      for (int u = 0; u < U; ++u) push_next(a, round + 1, want[u], y[u] >= 0 ? y[u] : 0);
-    }
-    if (!grid_barrier(st, gridDim.x)) return;
+    trace(round + 1, 3, global_timer_ns());
   }
   for (long long v = gthread; v < n; v += nthreads)
     if (__ldcg(a.m2 + v) < 0) a.m2[v] = (int)v;
   if (gthread == 0) st->rounds = round;
+  trace(0, 3, global_timer_ns());
+  trace(0, 4, (unsigned long long)round);
 }
 
 int64_t max_chunks(int64_t n, int64_t m) { return m / kChunk + n + 64; }
@@ -378,10 +432,9 @@ int64_t max_chunks(int64_t n, int64_t m) { return m / kChunk + n + 64; }
 
 size_t match_ws_bytes(int64_t n, int64_t m) {
   const int64_t ch = max_chunks(n, m);
-  size_t b = (size_t)n * 4 * 3;                               // ptr, stamp (+slack)
-  b += 2 * ((size_t)n * 4 * 4 + (size_t)ch * 4);              // two slots
-  b += (size_t)n * 4 * 4 + (size_t)ch * 4;                    // wake items + map
-  b += (size_t)ch * 4 * 3;                                    // partials
+  size_t b = (size_t)n * 4 * (3 + kTop);                      // ptr, stamp, top (+slack)
+  b += 2 * ((size_t)n * 4 * 6 + (size_t)ch * 4);              // two slots
+  b += (size_t)ch * 4 * 3 * kTop;                             // chunk partial lists
   return b + 64 * 256;
 }
 
@@ -405,6 +458,7 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
   };
   a.ptr = take((size_t)n * 4);
   a.stamp = take((size_t)n * 4);
+  a.top = take((size_t)n * 4 * kTop);
   for (int p = 0; p < 2; ++p) {
     Slot &S = a.slot[p];
     S.small = take((size_t)n * 4);
@@ -412,21 +466,19 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
     S.big_base = take((size_t)n * 4);
     S.big_done = take((size_t)n * 4);
     S.big_map = take((size_t)ch * 4);
+    S.upd = take((size_t)n * 4);
+    S.act = take((size_t)n * 4);
   }
-  a.wk_x = take((size_t)n * 4);
-  a.wk_v = take((size_t)n * 4);
-  a.wk_p = take((size_t)n * 4);
-  a.wk_base = take((size_t)n * 4);
-  a.wk_map = take((size_t)ch * 4);
-  a.part_w = take((size_t)ch * 4);
-  a.part_k = take((size_t)ch * 4);
-  a.part_h = (unsigned *)take((size_t)ch * 4);
+  a.part = take((size_t)ch * 4 * 3 * kTop);
   a.nsmall = take(64);
+  a.nupd = take(64);
+  a.nact = take(64);
   a.big = (unsigned long long *)take(64);
-  a.wk = (unsigned long long *)take(64);
   if (!ok) return cm_fail(CM_ERR_NOMEM, "cm_match: workspace too small");
   a.max_rounds = n + 8;
   a.st = ctx->d_status;
+  a.trace = ctx->d_trace;
+  a.trace_rows = ctx->trace_rows;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_match, kMatchThreads, 0);
   if (per_sm < 1) return cm_fail(CM_ERR_CUDA, "cm_match: kernel cannot be resident");

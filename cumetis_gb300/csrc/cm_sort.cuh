@@ -101,3 +101,73 @@ __device__ int block_merge_sort(K *k0, int *w0, K *k1, int *w1, int n, K pad) {
 }
 
 }  // namespace cm
+
+namespace cm {
+
+// Block merge sort of packed 64-bit words (sort key in the high bits, payload
+// in the low bits; ties among equal keys may end in any order).  One word per
+// entry halves the shared-memory traffic of the key/payload version, and the
+// merge keeps both run heads in registers so each output costs one load.
+// Returns 0 if the result is in a, 1 if in b.  All NT threads must call it.
+template <int NT, int E>
+__device__ int block_merge_sort_packed(unsigned long long *a, unsigned long long *b, int n) {
+  const int npad = ((n + E - 1) / E) * E;
+  for (int i = n + (int)threadIdx.x; i < npad; i += NT) a[i] = ~0ull;
+  __syncthreads();
+  const int nruns = npad / E;
+  for (int q = threadIdx.x; q < nruns; q += NT) {
+    unsigned long long v[E];
+#pragma unroll
+    for (int i = 0; i < E; ++i) v[i] = a[q * E + i];
+#pragma unroll
+    for (int size = 2; size <= E; size <<= 1) {
+#pragma unroll
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+          const int l = i ^ stride;
+          if (l > i) {
+            const bool up = (i & size) == 0;
+            if ((v[i] > v[l]) == up) { unsigned long long t = v[i]; v[i] = v[l]; v[l] = t; }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < E; ++i) a[q * E + i] = v[i];
+  }
+  __syncthreads();
+  unsigned long long *src = a, *dst = b;
+  int cur = 0;
+  for (int width = E; width < npad; width <<= 1) {
+    for (int q = threadIdx.x; q < nruns; q += NT) {
+      const int out = q * E;
+      const int ps = (out / (2 * width)) * (2 * width);
+      const int alen = min(width, npad - ps);
+      const int blen = min(width, npad - ps - alen);
+      const unsigned long long *A = src + ps;
+      const unsigned long long *B = A + alen;
+      const int diag = out - ps;
+      int i;
+      if (blen == 0) i = diag;
+      else if (A[alen - 1] <= B[0]) i = diag < alen ? diag : alen;
+      else i = merge_path(A, alen, B, blen, diag);
+      int j = diag - i;
+      unsigned long long ka = i < alen ? A[i] : ~0ull;
+      unsigned long long kb = j < blen ? B[j] : ~0ull;
+#pragma unroll
+      for (int t = 0; t < E; ++t) {
+        const bool takeA = (j >= blen) || (i < alen && ka <= kb);
+        dst[out + t] = takeA ? ka : kb;
+        if (takeA) { ++i; ka = i < alen ? A[i] : ~0ull; }
+        else { ++j; kb = j < blen ? B[j] : ~0ull; }
+      }
+    }
+    __syncthreads();
+    unsigned long long *t = src; src = dst; dst = t;
+    cur ^= 1;
+  }
+  return cur;
+}
+
+}  // namespace cm

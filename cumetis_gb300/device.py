@@ -74,6 +74,17 @@ class Context:
         _check(lib().cm_ctx_stage_times(self._h, buf, n, 1 if reset else 0))
         return {lib().cm_stage_name(i).decode(): float(buf[i]) for i in range(n)}
 
+    def set_match_trace(self, max_rounds):
+        _check(lib().cm_ctx_set_match_trace(self._h, int(max_rounds)))
+
+    def match_trace(self, cap_rows=4096):
+        """Rows of the last matching's trace (see cm_ctx_match_trace)."""
+        buf = (ctypes.c_int64 * (8 * cap_rows))()
+        rows = ctypes.c_int32(0)
+        _check(lib().cm_ctx_match_trace(self._h, buf, int(cap_rows), ctypes.byref(rows)))
+        a = np.frombuffer(buf, dtype=np.int64).reshape(cap_rows, 8)
+        return a[:rows.value].copy()
+
     def sync(self, stream=None):
         _check(lib().cm_ctx_sync(self._h, _stream_ptr(stream)))
 

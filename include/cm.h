@@ -128,6 +128,14 @@ enum {
   CM_STAGE_LONG_DEDUP = 4, CM_STAGE_TILES = 5, CM_STAGE_LONG_COPY = 6, CM_STAGE_COUNT = 7
 };
 int cm_ctx_set_stage_timing(cm_ctx *ctx, int enable);
+/* Matching trace: with max_rounds > 0 the next cm_match / cm_coarsen levels
+ * record, per handshake round, device timestamps (ns) of the phase starts and
+ * the round's work sizes.  cm_ctx_match_trace copies rows of 8 int64 of the
+ * last matching: row 0 = {kernel start, init done, round-0 start, end,
+ * rounds, 0, 0, 0}; row r+1 = {phase A, phase B, phase C, round end,
+ * lane-sized rows, chunked rows, row chunks, wake chunks}.  0 disables. */
+int cm_ctx_set_match_trace(cm_ctx *ctx, int32_t max_rounds);
+int cm_ctx_match_trace(cm_ctx *ctx, int64_t *out, int32_t cap_rows, int32_t *rows_out);
 int cm_ctx_stage_times(cm_ctx *ctx, double *ms, int32_t cap, int reset);
 const char *cm_stage_name(int32_t stage);
 

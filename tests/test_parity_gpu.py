@@ -161,11 +161,12 @@ def _long_row_graph(L_leader, L_follower, extra=0, seed=0):
     return O.CSR(np.cumsum(xadj), dst, w, np.ones(n))
 
 
-@pytest.mark.parametrize("lens", [(1024, 1024), (1024, 1025), (4096, 4096), (4097, 4096), (20000, 13000),
-                                  (40000, 30000)])
+@pytest.mark.parametrize("lens", [(512, 512), (512, 513), (1024, 1024), (1024, 1025), (2048, 2048), (2048, 2049),
+                                  (4096, 4096), (4097, 4096), (20000, 13000), (40000, 30000)])
 def test_long_rows(ctx, lens):
-    """Coarse rows around and far beyond the tile limit (2048) and the
-    long-row chunk (8192): exercises chunk sort, merge passes, dedup, copy."""
+    """Coarse rows at every path boundary: tile limit 1024, the size classes
+    2048 / 4096 / 8192, and far beyond the 8192-entry chunk (chunk sort,
+    merge passes, dedup, copy)."""
     g = _long_row_graph(*lens, extra=500, seed=sum(lens))
     match = np.arange(g.n, dtype=np.int32)
     match[0], match[1] = 1, 0
