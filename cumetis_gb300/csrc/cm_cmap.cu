@@ -27,7 +27,7 @@ k_cmap(int n, const int *__restrict__ xadj, const int *__restrict__ vwgt, const 
        int *__restrict__ cmap, int *__restrict__ leader, int *__restrict__ cvwgt, int *__restrict__ eoff,
        int *__restrict__ d_cnvtxs, int *__restrict__ long_list, int long_thr, unsigned long long *long_ctr,
        int long_chunk, int *__restrict__ chunk_row, int *__restrict__ first_row, int tile_diag,
-       int *__restrict__ mid_list, int *__restrict__ mid_ctr, int mid_cap,
+       int *__restrict__ mid_list, int *__restrict__ mid_ctr, int mid_cap, int4 *__restrict__ row_meta,
        unsigned long long *__restrict__ lb, DevStatus *st) {
   __shared__ int s_tile;
   __shared__ unsigned long long s_warp[kCmapThreads / 32];
@@ -83,9 +83,13 @@ k_cmap(int n, const int *__restrict__ xadj, const int *__restrict__ vwgt, const 
     if (v <= u) {
       const int c = (int)(P >> 31);
       const int e = (int)(P & kMask31);
-      const int L = (xadj[v + 1] - xadj[v]) + (u != v ? xadj[u + 1] - xadj[u] : 0);
+      const int xv = xadj[v], dv = xadj[v + 1] - xv;
+      const int xu = u != v ? xadj[u] : 0;
+      const int L = dv + (u != v ? xadj[u + 1] - xu : 0);
       cmap[v] = c;
       leader[c] = (int)v;
+      // contraction row metadata: leader's row start and length, follower's row start
+      if (row_meta) row_meta[c] = make_int4(xv, dv, xu, L);
       cvwgt[c] = (int)((unsigned)vwgt[v] + (u != v ? (unsigned)vwgt[u] : 0u));
       eoff[c] = e;
       if (first_row) {
@@ -144,7 +148,7 @@ int launch_cmap(cm_ctx *ctx, int32_t n, const int32_t *xadj, const int32_t *vwgt
                 int32_t *cmap, int32_t *leader, int32_t *cvwgt, int32_t *eoff, int32_t *d_cnvtxs,
                 int32_t *long_list, int32_t long_threshold, int32_t long_chunk, unsigned long long *d_long_ctr,
                 int32_t *chunk_row, int32_t *first_row, int32_t tile_diag, int32_t *mid_list, int32_t *mid_ctr,
-                int32_t mid_cap, cudaStream_t s) {
+                int32_t mid_cap, void *row_meta, cudaStream_t s) {
   if (n == 0) {
     cudaMemsetAsync(d_cnvtxs, 0, sizeof(int32_t), s);
     cudaMemsetAsync(eoff, 0, sizeof(int32_t), s);
@@ -158,8 +162,8 @@ int launch_cmap(cm_ctx *ctx, int32_t n, const int32_t *xadj, const int32_t *vwgt
   k_cmap<<<ntiles, kCmapThreads, 0, s>>>(n, xadj, vwgt, match, cmap, leader, cvwgt, eoff, d_cnvtxs, long_list,
                                           long_list ? long_threshold : INT32_MAX, d_long_ctr,
                                           long_chunk > 0 ? long_chunk : 1, chunk_row, first_row,
-                                          tile_diag > 0 ? tile_diag : 1, mid_list, mid_ctr, mid_cap, lb,
-                                          ctx->d_status);
+                                          tile_diag > 0 ? tile_diag : 1, mid_list, mid_ctr, mid_cap,
+                                          (int4 *)row_meta, lb, ctx->d_status);
   ctx->launches++;
   int blocks = ctx->num_sms * 8;
   k_cmap_followers<<<blocks, 256, 0, s>>>(n, match, cmap, ctx->d_status);
@@ -240,8 +244,8 @@ extern "C" int cm_build_cmap_noalloc(int32_t nvtxs, const int32_t *d_xadj, const
   // ticket and this call's tile words.
   cudaMemsetAsync(D.scratch, 0, (size_t)(kNoAllocStatusWords + ntiles + 1) * 8, s);
   k_cmap<<<ntiles, kCmapThreads, 0, s>>>(nvtxs, d_xadj, d_vwgt, d_match, d_cmap, d_leader, d_cvwgt, d_eoff, d_cnvtxs,
-                                          nullptr, INT32_MAX, nullptr, 1, nullptr, nullptr, 1, nullptr, nullptr, 0, lb,
-                                          st);
+                                          nullptr, INT32_MAX, nullptr, 1, nullptr, nullptr, 1, nullptr, nullptr, 0,
+                                          nullptr, lb, st);
   k_cmap_followers<<<D.num_sms * 8, 256, 0, s>>>(nvtxs, d_match, d_cmap, st);
   return cuda_status(cudaGetLastError(), "cm_build_cmap_noalloc launch");
 }

@@ -99,7 +99,8 @@ __global__ void __launch_bounds__(kTileThreads, sizeof(K) == 4 ? 6 : 3)
 k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
                  const int *__restrict__ match, const int *__restrict__ cmap, const int *__restrict__ leader,
                  const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
-                 const int *__restrict__ ucount, unsigned long long *lb, int *__restrict__ cxadj,
+                 const int4 *__restrict__ row_meta, const int *__restrict__ ucount, unsigned long long *lb,
+                 int *__restrict__ cxadj,
                  int *__restrict__ cadjncy, int *__restrict__ cadjwgt, int *d_sizes, DevStatus *st) {
   using KT = KeyT<K>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -137,14 +138,11 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
     const int r = tid * kRowsPerThread + i;
     int len = 0;
     if (r < R) {
-      const int c = clo + r;
-      const int l = leader[c];
-      const int f = match[l];
-      const int L = eoff[c + 1] - eoff[c];
-      const int xl = xadj[l];
-      S.r_xl[r] = xl;
-      S.r_dl[r] = xadj[l + 1] - xl;
-      S.r_xf[r] = f != l ? xadj[f] : 0;
+      const int4 md = row_meta[clo + r];  // (leader start, leader length, follower start, length)
+      const int L = md.w;
+      S.r_xl[r] = md.x;
+      S.r_dl[r] = md.y;
+      S.r_xf[r] = md.z;
       S.r_len[r] = L > kLongThr ? -1 : L;
       len = L > kLongThr ? 0 : L;
     }
@@ -323,18 +321,6 @@ struct RowSmem {
 };
 using ChunkSmem = RowSmem<kChunk>;
 
-__device__ __forceinline__ void long_row_info(const int *long_list, int idx, const int *leader, const int *match,
-                                              const int *xadj, const int *eoff, int &c, int &L, int &xl, int &dl,
-                                              int &xf) {
-  c = long_list[2 * idx];
-  const int l = leader[c];
-  const int f = match[l];
-  L = eoff[c + 1] - eoff[c];
-  xl = xadj[l];
-  dl = xadj[l + 1] - xl;
-  xf = f != l ? xadj[f] : 0;
-}
-
 // Passes a row of length L needs before its chunks form one sorted run.
 __host__ __device__ __forceinline__ int merge_passes(int L) {
   int p = 0;
@@ -418,22 +404,17 @@ template <int NT, int CAP>
 __global__ void __launch_bounds__(NT)
 k_mid_sort(const int *__restrict__ xadj, const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
            const int *__restrict__ match, const int *__restrict__ cmap, const int *__restrict__ leader,
-           const int *__restrict__ eoff, const int *__restrict__ list, const int *__restrict__ count,
-           int2 *__restrict__ stage1, int *__restrict__ ucount) {
+           const int *__restrict__ eoff, const int4 *__restrict__ row_meta, const int *__restrict__ list,
+           const int *__restrict__ count, int2 *__restrict__ stage1, int *__restrict__ ucount) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   RowSmem<CAP> &S = *reinterpret_cast<RowSmem<CAP> *>(smem_raw);
   __shared__ int scan[NT / 32 + 1];
   const int nrows = *count;
   for (int i = blockIdx.x; i < nrows; i += gridDim.x) {
     const int c = list[i];
-    const int l = leader[c];
-    const int f = match[l];
-    const int L = eoff[c + 1] - eoff[c];
-    const int xl = xadj[l];
-    const int dl = xadj[l + 1] - xl;
-    const int xf = f != l ? xadj[f] : 0;
-    sort_row_segment<NT, CAP>(S, scan, c, xl, dl, xf, 0, L, true, nullptr, stage1 + eoff[c], ucount + c, adjncy,
-                              adjwgt, cmap);
+    const int4 md = row_meta[c];
+    sort_row_segment<NT, CAP>(S, scan, c, md.x, md.y, md.z, 0, md.w, true, nullptr, stage1 + eoff[c], ucount + c,
+                              adjncy, adjwgt, cmap);
   }
 }
 
@@ -442,8 +423,8 @@ k_mid_sort(const int *__restrict__ xadj, const int *__restrict__ adjncy, const i
 __global__ void __launch_bounds__(kChunkThreads, 1)
 k_long_sort(const int *__restrict__ xadj, const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
             const int *__restrict__ match, const int *__restrict__ cmap, const int *__restrict__ leader,
-            const int *__restrict__ eoff, const int *__restrict__ long_list, const int *__restrict__ chunk_row,
-            const unsigned long long *long_ctr, int2 *__restrict__ stage) {
+            const int *__restrict__ eoff, const int4 *__restrict__ row_meta, const int *__restrict__ long_list,
+            const int *__restrict__ chunk_row, const unsigned long long *long_ctr, int2 *__restrict__ stage) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem &S = *reinterpret_cast<ChunkSmem *>(smem_raw);
   __shared__ int scan[kChunkThreads / 32 + 1];
@@ -451,13 +432,13 @@ k_long_sort(const int *__restrict__ xadj, const int *__restrict__ adjncy, const 
   const int nchunks = (int)(ctr & 0xffffffffu);
   for (int q = blockIdx.x; q < nchunks; q += gridDim.x) {
     const int idx = chunk_row[q];
-    int c, L, xl, dl, xf;
-    long_row_info(long_list, idx, leader, match, xadj, eoff, c, L, xl, dl, xf);
+    const int c = long_list[2 * idx];
+    const int4 md = row_meta[c];
     const int j = q - long_list[2 * idx + 1];
     const int cs = j * kChunk;
-    const int cnt = min(kChunk, L - cs);
-    sort_row_segment<kChunkThreads, kChunk>(S, scan, c, xl, dl, xf, cs, cnt, false, stage + eoff[c] + cs, nullptr,
-                                            nullptr, adjncy, adjwgt, cmap);
+    const int cnt = min(kChunk, md.w - cs);
+    sort_row_segment<kChunkThreads, kChunk>(S, scan, c, md.x, md.y, md.z, cs, cnt, false, stage + eoff[c] + cs,
+                                            nullptr, nullptr, adjncy, adjwgt, cmap);
   }
 }
 
@@ -617,6 +598,7 @@ size_t contract_ws_bytes(int64_t n, int64_t m) {
   b += (size_t)nchunks * 4 + 256;            // chunk_row
   b += 256;                                  // counters
   b += (size_t)(ntiles + 2) * 8 + 256;       // tile look-back
+  b += (size_t)n * 16 + 256;                 // row metadata
   b += (size_t)m * 8 * 2 + 512;              // stages
   b += cmap_ws_bytes(n);
   return b + 4096;
@@ -640,12 +622,13 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   int *long_list = (int *)ws_take(ctx, (size_t)(m / kChunk + 2) * 8);
   int *chunk_row = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
   int *mid_list = (int *)ws_take(ctx, (size_t)mid_cap * 3 * 4);
+  int4 *row_meta = (int4 *)ws_take(ctx, (size_t)n * 16);
   unsigned long long *ctr = (unsigned long long *)ws_take(ctx, 64);   // [0] chunked rows, [1] mid counters
   unsigned long long *lb = (unsigned long long *)ws_take(ctx, (size_t)(ntiles + 2) * 8);
   int2 *stage0 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
   int2 *stage1 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
-  if (!leader || !ucount || !eoff || !first_row || !long_list || !chunk_row || !mid_list || !ctr || !lb || !stage0 ||
-      !stage1)
+  if (!leader || !ucount || !eoff || !first_row || !long_list || !chunk_row || !mid_list || !row_meta || !ctr || !lb ||
+      !stage0 || !stage1)
     return cm_fail(CM_ERR_NOMEM, "contract: workspace too small");
   int *mid_ctr = reinterpret_cast<int *>(ctr + 1);
   DevStatus *st = ctx->d_status;
@@ -654,7 +637,7 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   cudaMemsetAsync(lb, 0, (size_t)(ntiles + 1) * 8, s);
   int rc = launch_cmap(ctx, (int32_t)n, fine->xadj, fine->vwgt, match, cmap, leader, coarse->vwgt, eoff,
                        d_sizes /* n' lands in d_sizes[0] */, long_list, kLongThr, kChunk, ctr, chunk_row, first_row,
-                       kTileDiag, mid_list, mid_ctr, (int32_t)mid_cap, s);
+                       kTileDiag, mid_list, mid_ctr, (int32_t)mid_cap, row_meta, s);
   if (rc) return rc;
   const int sms = ctx->num_sms;
   const bool small_ids = n < kSmallIdLimit;
@@ -679,17 +662,18 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   cudaEventRecord(ctx->fork_ev, s);
   for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(ctx->aux[i], ctx->fork_ev, 0);
   k_mid_sort<256, 2 * kLongThr><<<sms * 4, 256, sizeof(RowSmem<2 * kLongThr>), ctx->aux[0]>>>(
-      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, mid_list, mid_ctr + 0, stage1, ucount);
+      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, row_meta, mid_list, mid_ctr + 0, stage1,
+      ucount);
   k_mid_sort<512, 4 * kLongThr><<<sms * 2, 512, sizeof(RowSmem<4 * kLongThr>), ctx->aux[1]>>>(
-      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, mid_list + mid_cap, mid_ctr + 1, stage1,
-      ucount);
+      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, row_meta, mid_list + mid_cap, mid_ctr + 1,
+      stage1, ucount);
   k_mid_sort<1024, kChunk><<<sms, 1024, sizeof(RowSmem<kChunk>), ctx->aux[2]>>>(
-      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, mid_list + 2 * mid_cap, mid_ctr + 2, stage1,
-      ucount);
+      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, row_meta, mid_list + 2 * mid_cap,
+      mid_ctr + 2, stage1, ucount);
   ctx->launches += 3;
   for (int i = 0; i < 3; ++i) cudaEventRecord(ctx->join_ev[i], ctx->aux[i]);
   k_long_sort<<<sms, kChunkThreads, sizeof(ChunkSmem), s>>>(fine->xadj, fine->adjncy, fine->adjwgt, match, cmap,
-                                                           leader, eoff, long_list, chunk_row, ctr, stage0);
+                                                           leader, eoff, row_meta, long_list, chunk_row, ctr, stage0);
   ctx->launches++;
   {
     int per_sm = 0;
@@ -715,11 +699,11 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   stage_begin(ctx, s);
   if (small_ids)
     k_contract_tiles<unsigned><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
-        fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, d_sizes, first_row, ucount, lb,
+        fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, d_sizes, first_row, row_meta, ucount, lb,
         coarse->xadj, coarse->adjncy, coarse->adjwgt, d_sizes, st);
   else
     k_contract_tiles<unsigned long long><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
-        fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, d_sizes, first_row, ucount, lb,
+        fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, d_sizes, first_row, row_meta, ucount, lb,
         coarse->xadj, coarse->adjncy, coarse->adjwgt, d_sizes, st);
   stage_end(ctx, CM_STAGE_TILES, s);
   ctx->launches++;

@@ -300,7 +300,7 @@ extern "C" int cm_build_cmap(cm_ctx *ctx, int32_t nvtxs, const int32_t *d_xadj, 
   ws_reset(ctx);
   if ((rc = ws_ensure(ctx, cmap_ws_bytes(nvtxs)))) return rc;
   return launch_cmap(ctx, nvtxs, d_xadj, d_vwgt, d_match, d_cmap, d_leader, d_cvwgt, d_eoff, d_cnvtxs, nullptr, 0,
-                     1, nullptr, nullptr, nullptr, 0, nullptr, nullptr, 0, (cudaStream_t)stream);
+                     1, nullptr, nullptr, nullptr, 0, nullptr, nullptr, 0, nullptr, (cudaStream_t)stream);
 }
 
 extern "C" int cm_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *d_match, int32_t *d_cmap,

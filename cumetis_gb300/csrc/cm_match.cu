@@ -39,10 +39,12 @@ constexpr int kSerialDeg = 16;   // rows scanned by one lane
 constexpr int kChunk = 256;      // entries per warp work item
 constexpr int kTop = 4;          // cached candidates per vertex
 constexpr int kNotScanned = -2;  // top[v*kTop] before the first scan
+constexpr int kUnknown = -3;     // cache slot not computed (the first scan keeps only the best)
 
 struct Slot {      // lists feeding one round (double-buffered by round parity)
   int *small;      // full scans, rows <= kSerialDeg
-  int *big_v, *big_base, *big_done, *big_map;   // full scans, longer rows (chunked)
+  int *big_v, *big_base, *big_done;  // full scans, longer rows: vertex, first chunk, chunks done
+  int4 *desc;      // per chunk: (vertex, first entry, end entry, row index or -1 if one chunk)
   int *upd;        // pointers already updated from the cache
   int *act;        // active list for the round's phase C
 };
@@ -63,83 +65,133 @@ struct MatchArgs {
   int trace_rows;
 };
 
-struct Cand {
-  int w;
-  unsigned h;
-  int k;  // INT_MAX = none
-};
-
-__device__ __forceinline__ bool better(const Cand &a, const Cand &b) {
-  if (a.k == INT_MAX) return false;
-  if (b.k == INT_MAX) return true;
-  if (a.w != b.w) return a.w > b.w;
-  if (a.h != b.h) return a.h < b.h;
-  return a.k < b.k;
-}
-
-// Sorted (best first) list of up to kTop candidates held in registers.
-struct TopK {
-  Cand c[kTop];
-  __device__ __forceinline__ void clear() {
-#pragma unroll
-    for (int i = 0; i < kTop; ++i) c[i] = Cand{0, 0u, INT_MAX};
+// Candidates.  Lex mode (ties to the lower id) packs (weight, ~id) into one
+// 64-bit key, larger = better, 0 = none.  Hash mode compares (weight desc,
+// edge hash asc, id asc) field by field.
+template <bool H> struct Cand;
+template <> struct Cand<false> {
+  unsigned long long key = 0ull;
+  __device__ __forceinline__ static Cand make(int v, int k, int w) {
+    (void)v;
+    Cand c;
+    c.key = ((unsigned long long)((unsigned)w ^ 0x80000000u) << 32) | (unsigned)(~(unsigned)k);
+    return c;
   }
-  __device__ __forceinline__ void insert(const Cand &x) {
-    if (!better(x, c[kTop - 1])) return;
-    Cand cur = x;
+  __device__ __forceinline__ bool valid() const { return key != 0ull; }
+  __device__ __forceinline__ int id() const { return valid() ? (int)~(unsigned)key : -1; }
+  __device__ __forceinline__ bool better(const Cand &o) const { return key > o.key; }
+  __device__ __forceinline__ bool same(const Cand &o) const { return key == o.key; }
+  __device__ __forceinline__ Cand warp_best() const {
+    const unsigned hi = __reduce_max_sync(0xffffffffu, (unsigned)(key >> 32));
+    const unsigned lo = __reduce_max_sync(0xffffffffu, (unsigned)(key >> 32) == hi ? (unsigned)key : 0u);
+    Cand r;
+    r.key = ((unsigned long long)hi << 32) | lo;
+    return r;
+  }
+  __device__ __forceinline__ void store(int *p) const {
+    p[0] = (int)(unsigned)(key >> 32);
+    p[1] = (int)(unsigned)key;
+  }
+  __device__ __forceinline__ static Cand load(const int *p) {
+    Cand c;
+    c.key = ((unsigned long long)(unsigned)__ldcg(p) << 32) | (unsigned)__ldcg(p + 1);
+    return c;
+  }
+};
+template <> struct Cand<true> {
+  int w = 0;
+  unsigned h = 0u;
+  int k = INT_MAX;  // INT_MAX = none
+  __device__ __forceinline__ static Cand make(int v, int k, int w) {
+    Cand c;
+    c.w = w;
+    c.k = k;
+    c.h = edge_hash((unsigned)min(v, k), (unsigned)max(v, k));
+    return c;
+  }
+  __device__ __forceinline__ bool valid() const { return k != INT_MAX; }
+  __device__ __forceinline__ int id() const { return valid() ? k : -1; }
+  __device__ __forceinline__ bool better(const Cand &o) const {
+    if (k == INT_MAX) return false;
+    if (o.k == INT_MAX) return true;
+    if (w != o.w) return w > o.w;
+    if (h != o.h) return h < o.h;
+    return k < o.k;
+  }
+  __device__ __forceinline__ bool same(const Cand &o) const { return k == o.k && w == o.w && h == o.h; }
+  __device__ __forceinline__ Cand warp_best() const {
+    const unsigned full = 0xffffffffu;
+    const int wmax = __reduce_max_sync(full, valid() ? w : INT_MIN);
+    const bool atw = valid() && w == wmax;
+    const unsigned hmin = __reduce_min_sync(full, atw ? h : 0xffffffffu);
+    const bool ath = atw && h == hmin;
+    const unsigned kmin = __reduce_min_sync(full, ath ? (unsigned)k : 0xffffffffu);
+    Cand r;
+    r.w = wmax;
+    r.h = hmin;
+    r.k = kmin == 0xffffffffu ? INT_MAX : (int)kmin;
+    return r;
+  }
+  __device__ __forceinline__ void store(int *p) const {
+    p[0] = w;
+    p[1] = (int)h;
+    p[2] = k;
+  }
+  __device__ __forceinline__ static Cand load(const int *p) {
+    Cand c;
+    c.w = __ldcg(p);
+    c.h = (unsigned)__ldcg(p + 1);
+    c.k = __ldcg(p + 2);
+    return c;
+  }
+};
+constexpr int kPartInts = 3;  // ints per stored candidate (lex mode uses 2)
+
+// Sorted (best first) list of up to KK candidates held in registers.
+template <bool H, int KK>
+struct TopK {
+  Cand<H> c[KK];
+  __device__ __forceinline__ void insert(const Cand<H> &x) {
+    if (!x.better(c[KK - 1])) return;
+    Cand<H> cur = x;
 #pragma unroll
-    for (int i = 0; i < kTop; ++i) {
-      if (better(cur, c[i])) { Cand t = c[i]; c[i] = cur; cur = t; }
+    for (int i = 0; i < KK; ++i) {
+      if (cur.better(c[i])) { Cand<H> t = c[i]; c[i] = cur; cur = t; }
     }
   }
 };
 
-__device__ __forceinline__ bool eligible_cand(const MatchArgs &a, int v, long long vw, int k, int w, int s, Cand &out) {
+template <bool H>
+__device__ __forceinline__ bool eligible(const MatchArgs &a, long long vw, int v, int k, int s) {
+  (void)v;
   if (k == v || s >= 0) return false;  // self or matched
   const long long vk = -1ll - s;
   if (vw + vk > a.maxvwgt) return false;
-  if (!(3 * vw < a.maxvwgt || 3 * vk < a.maxvwgt)) return false;
-  out.w = w;
-  out.k = k;
-  out.h = a.mode == CM_MATCH_HEM_HASH ? edge_hash((unsigned)min(v, k), (unsigned)max(v, k)) : 0u;
-  return true;
+  return 3 * vw < a.maxvwgt || 3 * vk < a.maxvwgt;
 }
 
-__device__ __forceinline__ Cand warp_best(const Cand &c) {
-  const unsigned full = 0xffffffffu;
-  const bool valid = c.k != INT_MAX;
-  const int wmax = __reduce_max_sync(full, valid ? c.w : INT_MIN);
-  const bool atw = valid && c.w == wmax;
-  const unsigned hmin = __reduce_min_sync(full, atw ? c.h : 0xffffffffu);
-  const bool ath = atw && c.h == hmin;
-  const unsigned kmin = __reduce_min_sync(full, ath ? (unsigned)c.k : 0xffffffffu);
-  Cand r;
-  r.w = wmax;
-  r.h = hmin;
-  r.k = kmin == 0xffffffffu ? INT_MAX : (int)kmin;
-  return r;
-}
-
-// Merges the lanes' sorted lists into the warp's best kTop (all lanes get it).
-__device__ __forceinline__ TopK warp_topk(TopK t) {
-  TopK out;
+// Merges the lanes' sorted lists into the warp's best KK (all lanes get it).
+template <bool H, int KK>
+__device__ __forceinline__ TopK<H, KK> warp_topk(const TopK<H, KK> &t) {
+  TopK<H, KK> out;
   int head = 0;
 #pragma unroll
-  for (int i = 0; i < kTop; ++i) {
-    Cand mine = Cand{0, 0u, INT_MAX};
+  for (int i = 0; i < KK; ++i) {
+    Cand<H> mine;
 #pragma unroll
-    for (int j = 0; j < kTop; ++j)
+    for (int j = 0; j < KK; ++j)
       if (j == head) mine = t.c[j];
-    const Cand win = warp_best(mine);
+    const Cand<H> win = mine.warp_best();
     out.c[i] = win;
-    if (win.k != INT_MAX && mine.k == win.k && mine.w == win.w && mine.h == win.h) ++head;
+    if (win.valid() && mine.same(win)) ++head;
   }
   return out;
 }
 
-// Per-lane kTop over entries [b, e) (e - b <= kChunk) of v's row; all loads of
-// the chunk are issued before any is used.
-__device__ __forceinline__ TopK lane_scan(const MatchArgs &a, int v, long long vw, int b, int e) {
+// Per-lane best KK over entries [b, e) (e - b <= kChunk) of v's row; all loads
+// of the chunk are issued before any is used.
+template <bool H, int KK>
+__device__ __forceinline__ TopK<H, KK> lane_scan(const MatchArgs &a, int v, long long vw, int b, int e) {
   const int lane = threadIdx.x & 31;
   constexpr int U = kChunk / 32;
   int k[U], w[U], s[U];
@@ -151,24 +203,23 @@ __device__ __forceinline__ TopK lane_scan(const MatchArgs &a, int v, long long v
   }
 #pragma unroll
   for (int u = 0; u < U; ++u) s[u] = k[u] >= 0 ? __ldcg(a.m2 + k[u]) : 0;
-  TopK t;
-  t.clear();
+  TopK<H, KK> t;
 #pragma unroll
-  for (int u = 0; u < U; ++u) {
-    Cand c;
-    if (k[u] >= 0 && eligible_cand(a, v, vw, k[u], w[u], s[u], c)) t.insert(c);
-  }
+  for (int u = 0; u < U; ++u)
+    if (k[u] >= 0 && eligible<H>(a, vw, v, k[u], s[u])) t.insert(Cand<H>::make(v, k[u], w[u]));
   return t;
 }
 
-__device__ __forceinline__ void store_top(const MatchArgs &a, int v, const TopK &t) {
-  int4 q;
-  q.x = t.c[0].k == INT_MAX ? -1 : t.c[0].k;
-  q.y = t.c[1].k == INT_MAX ? -1 : t.c[1].k;
-  q.z = t.c[2].k == INT_MAX ? -1 : t.c[2].k;
-  q.w = t.c[3].k == INT_MAX ? -1 : t.c[3].k;
-  reinterpret_cast<int4 *>(a.top)[v] = q;
-  a.ptr[v] = q.x;
+// Writes v's cached candidate ids and points v at the first.  A first scan
+// (KK == 1) marks the rest of the cache unknown; a full list marks unused
+// slots "none" (the cache then holds every candidate).
+template <bool H, int KK>
+__device__ __forceinline__ void store_top(const MatchArgs &a, int v, const TopK<H, KK> &t) {
+  int q[kTop];
+#pragma unroll
+  for (int i = 0; i < kTop; ++i) q[i] = i < KK ? t.c[i].id() : (t.c[0].valid() ? kUnknown : -1);
+  reinterpret_cast<int4 *>(a.top)[v] = make_int4(q[0], q[1], q[2], q[3]);
+  a.ptr[v] = q[0];
 }
 
 __device__ __forceinline__ unsigned long long warp_excl_scan_u64(unsigned long long v, unsigned long long *total) {
@@ -189,8 +240,9 @@ __device__ __forceinline__ void warp_append(int *list, int *counter, bool take, 
   if (take) list[base + __popc(mask & ((1u << lane) - 1))] = x;
 }
 
-// Queues x (row of `deg` entries) for a full scan in slot `par`; convergent.
-__device__ __forceinline__ void append_scan(const MatchArgs &a, int par, bool take, int x, int deg) {
+// Queues x (row of `deg` entries starting at xs) for a full scan in slot
+// `par`; convergent.
+__device__ __forceinline__ void append_scan(const MatchArgs &a, int par, bool take, int x, int xs, int deg) {
   const Slot &S = a.slot[par];
   warp_append(S.small, a.nsmall + par, take && deg <= kSerialDeg, x);
   const bool bg = take && deg > kSerialDeg;
@@ -208,11 +260,35 @@ __device__ __forceinline__ void append_scan(const MatchArgs &a, int par, bool ta
     S.big_v[idx] = x;
     S.big_base[idx] = cb;
     S.big_done[idx] = 0;
-    for (int j = 0; j < nch; ++j) S.big_map[cb + j] = idx;
+    for (int j = 0; j < nch; ++j)
+      S.desc[cb + j] = make_int4(x, xs + j * kChunk, min(xs + deg, xs + (j + 1) * kChunk), nch > 1 ? idx : -1);
   }
 }
 
+// Block-aggregated append: every thread offers up to kCU items per list; one
+// atomicAdd per block and list.  All threads of the block must call it.
+constexpr int kCU = 4;  // vertices per thread in phase C
+__device__ __forceinline__ void block_append(int *list, int *counter, const bool (&take)[kCU], const int (&x)[kCU],
+                                             int *sh_scan, int *sh_base) {
+  int cnt = 0;
+#pragma unroll
+  for (int u = 0; u < kCU; ++u) cnt += take[u];
+  int total;
+  int ex = block_exclusive_scan<kMatchThreads>(cnt, sh_scan, &total);
+  if (threadIdx.x == 0) *sh_base = total ? atomicAdd(counter, total) : 0;
+  __syncthreads();
+  const int base = *sh_base + ex;
+  int o = 0;
+#pragma unroll
+  for (int u = 0; u < kCU; ++u)
+    if (take[u]) list[base + o++] = x[u];
+  __syncthreads();
+}
+
+template <bool H>
 __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
+  __shared__ int sh_scan[kMatchThreads / 32 + 1];
+  __shared__ int sh_base;
   const int lane = threadIdx.x & 31;
   const long long gthread = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nthreads = (long long)gridDim.x * blockDim.x;
@@ -241,8 +317,9 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
   // the vertex range, longer rows through the chunk list built here.
   for (long long b0 = (long long)gwarp * 32; b0 < n; b0 += (long long)nwarps * 32) {
     const long long v = b0 + lane;
-    const int deg = v < n ? a.xadj[v + 1] - a.xadj[v] : 0;
-    append_scan(a, 0, deg > kSerialDeg, (int)v, deg);
+    const int xs = v < n ? a.xadj[v] : 0;
+    const int deg = v < n ? a.xadj[v + 1] - xs : 0;
+    append_scan(a, 0, deg > kSerialDeg, (int)v, xs, deg);
   }
   if (!grid_barrier(st, gridDim.x)) return;
 
@@ -274,14 +351,17 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
       a.nact[par ^ 1] = 0;
       a.big[par ^ 1] = 0;
     }
+    // A vertex's first scan keeps only its best candidate (most vertices never
+    // need more); a rescan fills the whole cache.
+    const bool first = round == 0;
 
     // ---- phase A: full scans -------------------------------------------------
     for (long long b0 = (long long)gwarp * 32; b0 < nsmall; b0 += (long long)nwarps * 32) {
       const long long i = b0 + lane;
       if (i >= nsmall) continue;
-      const int v = round == 0 ? (int)i : __ldcg(S.small + i);
+      const int v = first ? (int)i : __ldcg(S.small + i);
       const int xs = a.xadj[v], deg = a.xadj[v + 1] - xs;
-      if (round == 0 && (deg == 0 || deg > kSerialDeg)) continue;
+      if (first && (deg == 0 || deg > kSerialDeg)) continue;
       const int sv = __ldcg(a.m2 + v);
       if (sv >= 0) continue;
       const long long vw = -1ll - sv;
@@ -290,39 +370,53 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
       for (int t = 0; t < kSerialDeg; ++t) k[t] = t < deg ? a.adjncy[xs + t] : -1;
 #pragma unroll
       for (int t = 0; t < kSerialDeg; ++t) s[t] = k[t] >= 0 ? __ldcg(a.m2 + k[t]) : 0;
-      TopK tk;
-      tk.clear();
+      if (first) {
+        TopK<H, 1> tk;
 #pragma unroll
-      for (int t = 0; t < kSerialDeg; ++t) {
-        Cand c;
-        if (k[t] >= 0 && eligible_cand(a, v, vw, k[t], a.adjwgt[xs + t], s[t], c)) tk.insert(c);
+        for (int t = 0; t < kSerialDeg; ++t)
+          if (k[t] >= 0 && eligible<H>(a, vw, v, k[t], s[t])) tk.insert(Cand<H>::make(v, k[t], a.adjwgt[xs + t]));
+        store_top(a, v, tk);
+      } else {
+        TopK<H, kTop> tk;
+#pragma unroll
+        for (int t = 0; t < kSerialDeg; ++t)
+          if (k[t] >= 0 && eligible<H>(a, vw, v, k[t], s[t])) tk.insert(Cand<H>::make(v, k[t], a.adjwgt[xs + t]));
+        store_top(a, v, tk);
       }
-      store_top(a, v, tk);
     }
     for (int q = gwarp; q < nchunks; q += nwarps) {
-      const int i = __ldcg(S.big_map + q);
-      const int v = __ldcg(S.big_v + i);
+      const int4 d = __ldcg(S.desc + q);
+      const int v = d.x, i = d.w;
       const int sv = __ldcg(a.m2 + v);
       if (sv >= 0) continue;  // uniform per warp
-      const int xs = a.xadj[v], xe = a.xadj[v + 1];
-      const int nch = (xe - xs + kChunk - 1) / kChunk;
-      const int j = q - __ldcg(S.big_base + i);
-      const int b = xs + j * kChunk, e = min(xe, b + kChunk);
-      const TopK r = warp_topk(lane_scan(a, v, -1ll - sv, b, e));
-      if (nch == 1) {
-        if (lane == 0) store_top(a, v, r);
+      const long long vw = -1ll - sv;
+      TopK<H, kTop> r;
+      if (first) {
+        const TopK<H, 1> r1 = warp_topk(lane_scan<H, 1>(a, v, vw, d.y, d.z));
+        r.c[0] = r1.c[0];
+      } else {
+        r = warp_topk(lane_scan<H, kTop>(a, v, vw, d.y, d.z));
+      }
+      if (i < 0) {  // the row's only chunk
+        if (lane == 0) {
+          if (first) {
+            TopK<H, 1> r1;
+            r1.c[0] = r.c[0];
+            store_top(a, v, r1);
+          } else {
+            store_top(a, v, r);
+          }
+        }
         continue;
       }
+      const int nch = (a.xadj[v + 1] - a.xadj[v] + kChunk - 1) / kChunk;
       int last = 0;
       if (lane < kTop) {
-        Cand mine = r.c[0];
+        Cand<H> mine = r.c[0];
 #pragma unroll
         for (int t = 1; t < kTop; ++t)
           if (lane == t) mine = r.c[t];
-        int *p = a.part + ((size_t)q * kTop + lane) * 3;
-        p[0] = mine.w;
-        p[1] = (int)mine.h;
-        p[2] = mine.k;
+        mine.store(a.part + ((size_t)q * kTop + lane) * kPartInts);
       }
       if (lane == 0) {
         __threadfence();
@@ -332,18 +426,19 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
       if (last) {  // merge the row's chunk lists
         __threadfence();
         const int base = __ldcg(S.big_base + i);
-        TopK acc;
-        acc.clear();
-        for (int t = lane; t < nch * kTop; t += 32) {
-          const int *p = a.part + ((size_t)base * kTop + t) * 3;
-          Cand o;
-          o.w = __ldcg(p);
-          o.h = (unsigned)__ldcg(p + 1);
-          o.k = __ldcg(p + 2);
-          acc.insert(o);
+        TopK<H, kTop> acc;
+        for (int t = lane; t < nch * kTop; t += 32)
+          acc.insert(Cand<H>::load(a.part + ((size_t)base * kTop + t) * kPartInts));
+        const TopK<H, kTop> rr = warp_topk(acc);
+        if (lane == 0) {
+          if (first) {
+            TopK<H, 1> r1;
+            r1.c[0] = rr.c[0];
+            store_top(a, v, r1);
+          } else {
+            store_top(a, v, rr);
+          }
         }
-        const TopK rr = warp_topk(acc);
-        if (lane == 0) store_top(a, v, rr);
       }
     }
     if (!grid_barrier(st, gridDim.x)) return;
@@ -355,8 +450,8 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
     for (long long i = gthread; i < tot_b; i += nthreads) {
       int v;
       if (i < nsmall) {
-        v = round == 0 ? (int)i : __ldcg(S.small + i);
-        if (round == 0) {
+        v = first ? (int)i : __ldcg(S.small + i);
+        if (first) {
           const int deg = a.xadj[v + 1] - a.xadj[v];
           if (deg == 0 || deg > kSerialDeg) continue;
         }
@@ -376,45 +471,71 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
     trace(round + 1, 2, global_timer_ns());
 
     // ---- phase C: filter the active list, refresh stale pointers -------------
-    for (long long b0 = (long long)gwarp * 32; b0 < nact; b0 += (long long)nwarps * 32) {
-      const long long i = b0 + lane;
-      int x = -1;
-      if (i < nact) {
-        x = round == 0 ? (int)i : __ldcg(S.act + i);
-        if (__ldcg(a.m2 + x) >= 0) x = -1;  // matched
+    // Blocks take kMatchThreads * kCU consecutive entries (block-wide appends).
+    const long long span = (long long)kMatchThreads * kCU;
+    for (long long b0 = (long long)blockIdx.x * span; b0 < nact; b0 += (long long)gridDim.x * span) {
+      int x[kCU], p[kCU], sx[kCU], sp[kCU];
+#pragma unroll
+      for (int u = 0; u < kCU; ++u) {
+        const long long i = b0 + threadIdx.x + (long long)kMatchThreads * u;
+        x[u] = i < nact ? (first ? (int)i : __ldcg(S.act + i)) : -1;
       }
-      const int p = x >= 0 ? __ldcg(a.ptr + x) : -1;
-      if (p < 0) x = -1;                   // no candidate: out for good
-      bool keep = false, upd = false, scan = false;
-      int deg = 0;
-      if (x >= 0) {
-        if (__ldcg(a.m2 + p) < 0) {
-          keep = true;                     // waiting on an unmatched candidate
-        } else {
-          const int4 c = reinterpret_cast<const int4 *>(a.top)[x];
-          const int cs[kTop] = {c.x, c.y, c.z, c.w};
-          int sm[kTop];
 #pragma unroll
-          for (int t = 0; t < kTop; ++t) sm[t] = cs[t] >= 0 ? __ldcg(a.m2 + cs[t]) : 0;
-          int np = -1;
+      for (int u = 0; u < kCU; ++u) {
+        sx[u] = x[u] >= 0 ? __ldcg(a.m2 + x[u]) : 0;
+        p[u] = x[u] >= 0 ? __ldcg(a.ptr + x[u]) : -1;
+      }
 #pragma unroll
-          for (int t = kTop - 1; t >= 0; --t)
-            if (cs[t] >= 0 && sm[t] < 0) np = cs[t];
-          if (np >= 0) {
-            a.ptr[x] = np;
-            keep = upd = true;
-          } else if (cs[kTop - 1] < 0) {
-            a.ptr[x] = -1;                 // cache held every candidate: none left
-          } else {
-            keep = scan = true;
-            deg = a.xadj[x + 1] - a.xadj[x];
-          }
+      for (int u = 0; u < kCU; ++u)
+        if (sx[u] >= 0 || p[u] < 0) x[u] = -1;  // matched, or no candidate: out for good
+#pragma unroll
+      for (int u = 0; u < kCU; ++u) sp[u] = x[u] >= 0 ? __ldcg(a.m2 + p[u]) : -1;
+      bool keep[kCU], upd[kCU], scan[kCU];
+      int xs[kCU], deg[kCU];
+#pragma unroll
+      for (int u = 0; u < kCU; ++u) {
+        keep[u] = upd[u] = scan[u] = false;
+        xs[u] = deg[u] = 0;
+        const int xv = x[u];
+        if (xv < 0) continue;
+        if (sp[u] < 0) {
+          keep[u] = true;                    // waiting on an unmatched candidate
+          continue;
         }
+        const int4 c = reinterpret_cast<const int4 *>(a.top)[xv];
+        const int cs[kTop] = {c.x, c.y, c.z, c.w};
+        int sm[kTop];
+#pragma unroll
+        for (int t = 0; t < kTop; ++t) sm[t] = cs[t] >= 0 ? __ldcg(a.m2 + cs[t]) : 0;
+        // first unmatched cached candidate; -1 = no candidate left, kUnknown or
+        // a full cache exhausted = rescan
+        int np = -2;
+#pragma unroll
+        for (int t = kTop - 1; t >= 0; --t) {
+          if (cs[t] >= 0 && sm[t] < 0) np = cs[t];
+          else if (cs[t] == -1) np = -1;
+          else if (cs[t] == kUnknown) np = -2;
+        }
+        if (np >= 0) {
+          a.ptr[xv] = np;
+          keep[u] = upd[u] = true;
+        } else if (np == -1) {
+          a.ptr[xv] = -1;                    // the cache held every candidate: none left
+        } else {
+          keep[u] = scan[u] = true;
+          xs[u] = a.xadj[xv];
+          deg[u] = a.xadj[xv + 1] - xs[u];
+        }
+        if (upd[u] || scan[u]) atomicMax(a.stamp + xv, round + 1);
       }
-      if (upd || scan) atomicMax(a.stamp + x, round + 1);
-      warp_append(N.act, a.nact + (par ^ 1), keep, x);
-      warp_append(N.upd, a.nupd + (par ^ 1), upd, x);
-      append_scan(a, par ^ 1, scan, x, deg);
+      bool small[kCU];
+#pragma unroll
+      for (int u = 0; u < kCU; ++u) small[u] = scan[u] && deg[u] <= kSerialDeg;
+      block_append(N.act, a.nact + (par ^ 1), keep, x, sh_scan, &sh_base);
+      block_append(N.upd, a.nupd + (par ^ 1), upd, x, sh_scan, &sh_base);
+      block_append(N.small, a.nsmall + (par ^ 1), small, x, sh_scan, &sh_base);
+#pragma unroll
+      for (int u = 0; u < kCU; ++u) append_scan(a, par ^ 1, scan[u] && !small[u], x[u], xs[u], deg[u]);
     }
     if (!grid_barrier(st, gridDim.x)) return;
     trace(round + 1, 3, global_timer_ns());
@@ -433,8 +554,8 @@ int64_t max_chunks(int64_t n, int64_t m) { return m / kChunk + n + 64; }
 size_t match_ws_bytes(int64_t n, int64_t m) {
   const int64_t ch = max_chunks(n, m);
   size_t b = (size_t)n * 4 * (3 + kTop);                      // ptr, stamp, top (+slack)
-  b += 2 * ((size_t)n * 4 * 6 + (size_t)ch * 4);              // two slots
-  b += (size_t)ch * 4 * 3 * kTop;                             // chunk partial lists
+  b += 2 * ((size_t)n * 4 * 6 + (size_t)ch * 16);             // two slots
+  b += (size_t)ch * 4 * kPartInts * kTop;                     // chunk partial lists
   return b + 64 * 256;
 }
 
@@ -465,11 +586,11 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
     S.big_v = take((size_t)n * 4);
     S.big_base = take((size_t)n * 4);
     S.big_done = take((size_t)n * 4);
-    S.big_map = take((size_t)ch * 4);
+    S.desc = (int4 *)take((size_t)ch * 16);
     S.upd = take((size_t)n * 4);
     S.act = take((size_t)n * 4);
   }
-  a.part = take((size_t)ch * 4 * 3 * kTop);
+  a.part = take((size_t)ch * 4 * kPartInts * kTop);
   a.nsmall = take(64);
   a.nupd = take(64);
   a.nact = take(64);
@@ -480,12 +601,13 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
   a.trace = ctx->d_trace;
   a.trace_rows = ctx->trace_rows;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_match, kMatchThreads, 0);
+  const void *fn = mode == CM_MATCH_HEM_HASH ? (const void *)k_match<true> : (const void *)k_match<false>;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kMatchThreads, 0);
   if (per_sm < 1) return cm_fail(CM_ERR_CUDA, "cm_match: kernel cannot be resident");
   const int grid = ctx->num_sms * per_sm;
   void *args[] = {(void *)&a};
   stage_begin(ctx, s);
-  cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_match, dim3(grid), dim3(kMatchThreads), args, 0, s);
+  cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kMatchThreads), args, 0, s);
   stage_end(ctx, CM_STAGE_MATCH, s);
   if (e != cudaSuccess) return cuda_status(e, "cm_match launch");
   ctx->launches++;
