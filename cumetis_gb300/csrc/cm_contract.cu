@@ -15,16 +15,20 @@
 // Work split by expanded coarse-row length L = deg(leader) + deg(follower):
 //   L <= kLongThr : contraction tiles.  Tile k owns the rows whose diagonal
 //                   c + eoff[c] lies in [kD, (k+1)D) (D = kTileDiag), so a tile
-//                   holds <= D rows and < D + kLongThr entries.  The entries
-//                   are gathered into shared memory, sorted by (row, coarse id)
-//                   with a block merge sort, merged, and written once to their
-//                   final place; a decoupled look-back over tiles yields the
-//                   output offsets (the "one more scan" for cxadj).
-//   L >  kLongThr : long rows.  Chunks of kChunk entries are sorted in shared
-//                   memory into a global stage, merged pairwise (merge path, all
-//                   blocks cooperating, one grid barrier per pass), deduplicated,
-//                   and copied to their final place once the tiles have fixed
-//                   the offsets.
+//                   holds <= D rows and < D + kLongThr entries.  Two passes:
+//                   the count pass gathers the tile's entries and counts each
+//                   row's distinct coarse ids with a shared-memory hash set; a
+//                   scan of the counts gives cxadj (the "one more scan"); the
+//                   emit pass gathers again, sorts by (row, coarse id) with a
+//                   block merge sort, merges duplicates and writes each entry
+//                   once to its final place.
+//   L >  kLongThr : long rows, beside the count pass on auxiliary streams.
+//                   Rows up to kChunk entries: one block sorts and merges a
+//                   row (three size classes).  Longer rows: chunks of kChunk
+//                   entries are sorted in shared memory into a global stage,
+//                   merged pairwise (merge path, all blocks cooperating, one
+//                   grid barrier per pass) and deduplicated.  Their unique
+//                   entries are copied out beside the emit pass.
 #include "cm_ctx.h"
 #include "cm_sort.cuh"
 
@@ -36,6 +40,7 @@ constexpr int kTileE = 4;
 constexpr int kTileDiag = 512;                    // D
 constexpr int kLongThr = 1024;                    // rows longer than this take the long path
 constexpr int kTileCap = kTileDiag + kLongThr;    // max entries in a tile (multiple of kTileE)
+constexpr int kHashCap = 4096;                    // count-pass hash slots (power of two >= 2 kTileCap)
 constexpr int kChunk = 8192;                      // long-row chunk (entries sorted per block)
 constexpr int kChunkThreads = 1024;
 constexpr unsigned kSelfKey = 0xffffffffu;        // self loops sort last in their row
@@ -63,22 +68,8 @@ template <> struct KeyT<unsigned long long> {
   static __device__ __forceinline__ unsigned id(unsigned long long k) { return (unsigned)k; }
 };
 constexpr int kSmallIdLimit = (1 << 23) - 1;   // n below this uses 32-bit keys
+static_assert(kHashCap >= 2 * kTileCap && (kHashCap & (kHashCap - 1)) == 0, "count hash: power of two >= 2 cap");
 static_assert(kTileDiag <= 512, "tile rows must fit in 9 bits");
-
-template <typename K>
-struct TileSmem {
-  // k0/w0: gathered entries; k1/w1: sort scratch, and before the sort the
-  // hash table that counts unique (row, id) keys (contiguous: 12 or 8 bytes
-  // per tile entry).
-  K k0[kTileCap];
-  int w0[kTileCap];
-  K k1[kTileCap];
-  int w1[kTileCap];
-  int r_xl[kTileDiag], r_dl[kTileDiag], r_xf[kTileDiag], r_start[kTileDiag], r_len[kTileDiag], r_c[kTileDiag];
-  int scan[kTileThreads / 32 + 1];
-  int s_tile, s_clo, s_chi;
-  unsigned long long s_base;
-};
 
 __device__ __forceinline__ int upper_bound_smem(const int *a, int n, int x) {
   int lo = 0, hi = n;
@@ -94,42 +85,26 @@ __device__ __forceinline__ int upper_bound_smem(const int *a, int n, int x) {
 // (as find_cnvtxsedge_original places them, cuMetis.cu:1014-1020).
 __device__ __forceinline__ int expanded_src(int o, int xl, int dl, int xf) { return o < dl ? xl + o : xf + (o - dl); }
 
-template <typename K>
-__global__ void __launch_bounds__(kTileThreads, sizeof(K) == 4 ? 6 : 3)
-k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
-                 const int *__restrict__ match, const int *__restrict__ cmap, const int *__restrict__ leader,
-                 const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
-                 const int4 *__restrict__ row_meta, const int *__restrict__ ucount, unsigned long long *lb,
-                 int *__restrict__ cxadj,
-                 int *__restrict__ cadjncy, int *__restrict__ cadjwgt, int *d_sizes, DevStatus *st) {
-  using KT = KeyT<K>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  TileSmem<K> &S = *reinterpret_cast<TileSmem<K> *>(smem_raw);
-  // 32-bit keys: (k0, w0) and (k1, w1) are used as packed 64-bit words
-  // (key << 32 | weight), sorted as one array each.
-  constexpr bool kPacked = sizeof(K) == 4;
-  unsigned long long *P0 = reinterpret_cast<unsigned long long *>(S.k0);
-  unsigned long long *P1 = reinterpret_cast<unsigned long long *>(S.k1);
+// Per-tile row table shared by the count and emit passes.
+struct TileRows {
+  int r_xl[kTileDiag], r_dl[kTileDiag], r_xf[kTileDiag], r_start[kTileDiag], r_len[kTileDiag];
+  int scan[kTileThreads / 32 + 1];
+};
+
+// Rows [clo, clo+R) of tile t (rows whose diagonal c + eoff[c] lies in
+// [tD, (t+1)D)); loads their metadata and lays the short rows' entries out
+// back to back (long rows take no space).  Returns the number of entries.
+__device__ __forceinline__ int tile_rows(TileRows &T, int tile, int nc, long long dend, const int *first_row,
+                                         const int4 *row_meta, int &clo, int &R, DevStatus *st) {
   const int tid = threadIdx.x;
-  const int nc = *d_cn;
-  const long long m = eoff[nc];
-  const long long dend = (long long)nc + m;
-  if (tid == 0) {
-    const int t = (int)atomicAdd(lb, 1ull);
-    S.s_tile = t;
-    const long long last = dend / kTileDiag;
-    S.s_clo = t <= last ? first_row[t] : nc;
-    S.s_chi = t + 1 <= last ? first_row[t + 1] : nc;
-  }
-  __syncthreads();
-  const int tile = S.s_tile, clo = S.s_clo;
-  int R = S.s_chi - clo;
+  const long long last = dend / kTileDiag;
+  clo = tile <= last ? first_row[tile] : nc;
+  const int chi = tile + 1 <= last ? first_row[tile + 1] : nc;
+  R = chi - clo;
   if (R < 0 || R > kTileDiag) {  // inconsistent tile map: report, touch nothing
     if (tid == 0) record_error(st, CM_ERR_INVALID, ERR_SITE_BOUNDS);
     R = 0;
   }
-
-  // Row metadata: 4 consecutive rows per thread (independent load chains).
   constexpr int kRowsPerThread = kTileDiag / kTileThreads;
   int lens[kRowsPerThread];
   int mysum = 0;
@@ -139,18 +114,17 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
     int len = 0;
     if (r < R) {
       const int4 md = row_meta[clo + r];  // (leader start, leader length, follower start, length)
-      const int L = md.w;
-      S.r_xl[r] = md.x;
-      S.r_dl[r] = md.y;
-      S.r_xf[r] = md.z;
-      S.r_len[r] = L > kLongThr ? -1 : L;
-      len = L > kLongThr ? 0 : L;
+      T.r_xl[r] = md.x;
+      T.r_dl[r] = md.y;
+      T.r_xf[r] = md.z;
+      T.r_len[r] = md.w > kLongThr ? -1 : md.w;
+      len = md.w > kLongThr ? 0 : md.w;
     }
     lens[i] = len;
     mysum += len;
   }
   int ntot;
-  int ex = block_exclusive_scan<kTileThreads>(mysum, S.scan, &ntot);
+  int ex = block_exclusive_scan<kTileThreads>(mysum, T.scan, &ntot);
   const bool overflow = ntot > kTileCap;
   if (overflow) {
     if (tid == 0) record_error(st, CM_ERR_INVALID, ERR_SITE_BOUNDS);
@@ -159,90 +133,206 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
 #pragma unroll
   for (int i = 0; i < kRowsPerThread; ++i) {
     const int r = tid * kRowsPerThread + i;
-    if (r < R) S.r_start[r] = overflow ? 0 : ex;
-    if (r < R && overflow) S.r_len[r] = 0;
+    if (r < R) T.r_start[r] = overflow ? 0 : ex;
+    if (r < R && overflow) T.r_len[r] = 0;
     ex += lens[i];
   }
   __syncthreads();
+  return ntot;
+}
 
-  // Gather (row, cmap[x]) keys and weights, 4 entries in flight per thread;
-  // consecutive entries of a fine row go to consecutive lanes (coalesced).
-  for (int e0 = tid; e0 < ntot; e0 += 4 * kTileThreads) {
-    int src[4], rr[4], x[4], w[4];
+// Gathers 4 entries per thread per step: row, coarse id (self loops marked)
+// and weight of expanded entries e0 + u*kTileThreads; consecutive entries of a
+// fine row go to consecutive lanes (coalesced adjncy/adjwgt reads).
+__device__ __forceinline__ void tile_gather4(const TileRows &T, int R, int clo, int ntot, int e0,
+                                             const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
+                                             const int *__restrict__ cmap, int (&rr)[4], int (&id)[4], int (&w)[4],
+                                             unsigned selfkey) {
+  int src[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int e = e0 + u * kTileThreads;
-      rr[u] = 0;
-      src[u] = -1;
-      if (e < ntot) {
-        const int r = upper_bound_smem(S.r_start, R, e) - 1;
-        rr[u] = r;
-        src[u] = expanded_src(e - S.r_start[r], S.r_xl[r], S.r_dl[r], S.r_xf[r]);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      x[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
-      w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : 0;
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int e = e0 + u * kTileThreads;
-      if (e < ntot) {
-        const unsigned id = (x[u] == clo + rr[u]) ? KT::kSelf : (unsigned)x[u];
-        if constexpr (kPacked) {
-          P0[e] = ((unsigned long long)KT::make(rr[u], id) << 32) | (unsigned)w[u];
-        } else {
-          S.k0[e] = KT::make(rr[u], id);
-          S.w0[e] = w[u];
-        }
-      }
+  for (int u = 0; u < 4; ++u) {
+    const int e = e0 + u * kTileThreads;
+    rr[u] = 0;
+    src[u] = -1;
+    if (e < ntot) {
+      const int r = upper_bound_smem(T.r_start, R, e) - 1;
+      rr[u] = r;
+      src[u] = expanded_src(e - T.r_start[r], T.r_xl[r], T.r_dl[r], T.r_xf[r]);
     }
   }
-  // Count unique non-self keys with a shared-memory hash set, so that the
-  // tile's aggregate is published before the (longer) sort: later tiles never
-  // wait on this tile's sort in their look-back.
-  constexpr int kHash = (int)((sizeof(K) + 4) * kTileCap / sizeof(K));
-  const unsigned hsize = (unsigned)min(kHash, 2 * ntot + 1);  // load factor <= 1/2 (2/3 for 64-bit keys)
-  K *tab = S.k1;
-  for (int i = tid; i < (int)hsize; i += kTileThreads) tab[i] = KT::kPad;
-  int long_sum = 0;
 #pragma unroll
-  for (int i = 0; i < kRowsPerThread; ++i) {
-    const int r = tid * kRowsPerThread + i;
-    if (r < R && S.r_len[r] < 0) long_sum += ucount[clo + r];
+  for (int u = 0; u < 4; ++u) {
+    id[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
+    w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) id[u] = src[u] >= 0 ? cmap[id[u]] : 0;
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+    if (src[u] >= 0 && id[u] == clo + rr[u]) id[u] = (int)selfkey;
+}
+
+// Pass 1: unique coarse ids per short row, counted with a shared-memory hash
+// set of (row, id) keys; writes ucount[c].  No sort, no look-back.
+template <typename K>
+struct CountSmem {
+  TileRows T;
+  K tab[kHashCap];
+  int cnt[kTileDiag];
+};
+
+template <typename K>
+__global__ void __launch_bounds__(kTileThreads)
+k_tile_count(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
+             const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
+             const int4 *__restrict__ row_meta, int *__restrict__ ucount, DevStatus *st) {
+  using KT = KeyT<K>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  CountSmem<K> &S = *reinterpret_cast<CountSmem<K> *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int nc = *d_cn;
+  const long long dend = (long long)nc + eoff[nc];
+  int clo, R;
+  const int ntot = tile_rows(S.T, blockIdx.x, nc, dend, first_row, row_meta, clo, R, st);
+  unsigned hsize = 64;
+  while (hsize < (unsigned)(2 * ntot)) hsize <<= 1;  // <= kHashCap since ntot <= kTileCap
+  const unsigned hmask = hsize - 1;
+  for (int i = tid; i < (int)hsize; i += kTileThreads) S.tab[i] = KT::kPad;
+  for (int r = tid; r < R; r += kTileThreads) S.cnt[r] = 0;
+  __syncthreads();
+  for (int e0 = tid; e0 < ntot; e0 += 4 * kTileThreads) {
+    int rr[4], id[4], w[4];
+    tile_gather4(S.T, R, clo, ntot, e0, adjncy, adjwgt, cmap, rr, id, w, KT::kSelf);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (e0 + u * kTileThreads >= ntot || (unsigned)id[u] == KT::kSelf) continue;
+      const K key = KT::make(rr[u], (unsigned)id[u]);
+      unsigned h = (unsigned)(((unsigned long long)key * 0x9E3779B97F4A7C15ull) >> 40) & hmask;
+      for (unsigned probe = 0; probe < hsize; ++probe) {
+        const K old = atomicCAS(&S.tab[h], KT::kPad, key);
+        if (old == KT::kPad) { atomicAdd(&S.cnt[rr[u]], 1); break; }
+        if (old == key) break;
+        h = (h + 1) & hmask;
+      }
+    }
   }
   __syncthreads();
-  int uniq = long_sum;
-  for (int e = tid; e < ntot; e += kTileThreads) {
-    const K key = kPacked ? (K)(P0[e] >> 32) : S.k0[e];
-    if (KT::id(key) == KT::kSelf) continue;
-    unsigned h = (unsigned)(((unsigned long long)key * 0x9E3779B97F4A7C15ull) >> 32) % hsize;
-    for (unsigned probe = 0; probe < hsize; ++probe) {
-      const K old = atomicCAS(&tab[h], KT::kPad, key);
-      if (old == KT::kPad) { ++uniq; break; }
-      if (old == key) break;
-      h = h + 1 == hsize ? 0u : h + 1;
+  for (int r = tid; r < R; r += kTileThreads)
+    if (S.T.r_len[r] >= 0) ucount[clo + r] = S.cnt[r];
+}
+
+// Exclusive scan of the per-row unique counts into cxadj (decoupled look-back
+// over 2048-row tiles); d_sizes[1] = m'.
+constexpr int kScanThreads = 256, kScanItems = 8;
+__global__ void __launch_bounds__(kScanThreads)
+k_count_scan(const int *__restrict__ ucount, const int *d_cn, int *__restrict__ cxadj, int *d_sizes,
+             unsigned long long *lb, DevStatus *st) {
+  __shared__ int s_tile;
+  __shared__ unsigned long long s_warp[kScanThreads / 32];
+  __shared__ unsigned long long s_excl;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nc = *d_cn;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(lb, 1ull);
+  __syncthreads();
+  const int tile = s_tile;
+  const long long base = (long long)tile * kScanThreads * kScanItems + (long long)threadIdx.x * kScanItems;
+  int v[kScanItems];
+  unsigned long long sum = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    v[i] = base + i < nc ? ucount[base + i] : 0;
+    sum += (unsigned)v[i];
+  }
+  const unsigned long long inc = warp_inclusive_scan_u64(sum);
+  if (lane == 31) s_warp[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    const unsigned long long x = lane < kScanThreads / 32 ? s_warp[lane] : 0ull;
+    const unsigned long long xi = warp_inclusive_scan_u64(x);
+    const unsigned long long agg = __shfl_sync(0xffffffffu, xi, kScanThreads / 32 - 1);
+    if (lane < kScanThreads / 32) s_warp[lane] = xi - x;
+    const unsigned long long ex = lookback_exclusive(lb, tile, agg, st);
+    if (lane == 0) s_excl = ex;
+  }
+  __syncthreads();
+  unsigned long long run = s_excl + s_warp[wid] + inc - sum;
+  if (tile == 0 && threadIdx.x == 0) cxadj[0] = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    if (base + i >= nc) break;
+    run += (unsigned)v[i];
+    cxadj[base + i + 1] = (int)run;
+    if (base + i == nc - 1) d_sizes[1] = (int)run;
+  }
+}
+
+// Pass 2: gathers each tile's entries again, sorts them by (row, coarse id),
+// merges duplicates and writes every unique entry to its final place
+// cxadj[row] + rank.
+template <typename K>
+struct EmitSmem;
+template <>
+struct EmitSmem<unsigned> {  // packed (row:9 | id:23) << 32 | weight, padded layout
+  TileRows T;
+  int r_out[kTileDiag];
+  unsigned long long p[2][padded_size(kTileCap + 8)];
+};
+template <>
+struct EmitSmem<unsigned long long> {  // 64-bit (row, id) keys with separate weights
+  TileRows T;
+  int r_out[kTileDiag];
+  unsigned long long k[2][kTileCap];
+  int w[2][kTileCap];
+};
+
+template <typename K>
+__global__ void __launch_bounds__(kTileThreads)
+k_tile_emit(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
+            const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
+            const int4 *__restrict__ row_meta, const int *__restrict__ cxadj, int *__restrict__ cadjncy,
+            int *__restrict__ cadjwgt, DevStatus *st) {
+  using KT = KeyT<K>;
+  constexpr bool kPacked = sizeof(K) == 4;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  EmitSmem<K> &S = *reinterpret_cast<EmitSmem<K> *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int nc = *d_cn;
+  const long long dend = (long long)nc + eoff[nc];
+  int clo, R;
+  const int ntot = tile_rows(S.T, blockIdx.x, nc, dend, first_row, row_meta, clo, R, st);
+  for (int r = tid; r < R; r += kTileThreads) S.r_out[r] = cxadj[clo + r];
+  for (int e0 = tid; e0 < ntot; e0 += 4 * kTileThreads) {
+    int rr[4], id[4], w[4];
+    tile_gather4(S.T, R, clo, ntot, e0, adjncy, adjwgt, cmap, rr, id, w, KT::kSelf);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int e = e0 + u * kTileThreads;
+      if (e >= ntot) continue;
+      if constexpr (kPacked) {
+        S.p[0][pad16(e)] = ((unsigned long long)KT::make(rr[u], (unsigned)id[u]) << 32) | (unsigned)w[u];
+      } else {
+        S.k[0][e] = KT::make(rr[u], (unsigned)id[u]);
+        S.w[0][e] = w[u];
+      }
     }
   }
-  int agg;
-  block_exclusive_scan<kTileThreads>(uniq, S.scan, &agg);
-  if (tid < 32) lookback_publish(lb, tile, (unsigned long long)agg);
   __syncthreads();
   int b;
-  if constexpr (kPacked) b = block_merge_sort_packed<kTileThreads, kTileE>(P0, P1, ntot);
-  else b = block_merge_sort<K, kTileThreads, kTileE>(S.k0, S.w0, S.k1, S.w1, ntot, KT::kPad);
-  const unsigned long long *Ps = b ? P1 : P0;
-  const K *Kw = b ? S.k1 : S.k0;
-  const int *Ww = b ? S.w1 : S.w0;
-  auto keyat = [&](int i) -> K { if constexpr (kPacked) return (K)(Ps[i] >> 32); else return Kw[i]; };
-  auto wat = [&](int i) -> int { if constexpr (kPacked) return (int)(unsigned)Ps[i]; else return Ww[i]; };
-  int *hs = reinterpret_cast<int *>(b ? S.k0 : S.k1);  // exclusive head count, ntot + 1 ints
-
-  // Heads (first of a run of equal (row, id), not a self loop): one block scan
-  // over per-thread contiguous chunks.
+  if constexpr (kPacked) b = block_merge_sort_packed<kTileThreads, kTileE>(S.p[0], S.p[1], ntot);
+  else b = block_merge_sort<K, kTileThreads, kTileE>(S.k[0], S.w[0], S.k[1], S.w[1], ntot, KT::kPad);
+  auto keyat = [&](int i) -> K {
+    if constexpr (kPacked) return (K)(S.p[b][pad16(i)] >> 32);
+    else return S.k[b][i];
+  };
+  auto wat = [&](int i) -> int {
+    if constexpr (kPacked) return (int)(unsigned)S.p[b][pad16(i)];
+    else return S.w[b][i];
+  };
+  int *hs;
+  if constexpr (kPacked) hs = reinterpret_cast<int *>(S.p[b ^ 1]);
+  else hs = reinterpret_cast<int *>(S.k[b ^ 1]);
+  // heads (first of a run of equal (row, id), not a self loop), one block scan
+  // over per-thread contiguous chunks
   const int ipt = (ntot + kTileThreads - 1) / kTileThreads;
   const int i0 = min(ntot, tid * ipt), i1 = min(ntot, i0 + ipt);
   int hcnt = 0;
@@ -251,7 +341,7 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
     hcnt += (KT::id(k) != KT::kSelf) && (i == 0 || keyat(i - 1) != k);
   }
   int htot;
-  int run = block_exclusive_scan<kTileThreads>(hcnt, S.scan, &htot);
+  int run = block_exclusive_scan<kTileThreads>(hcnt, S.T.scan, &htot);
   for (int i = i0; i < i1; ++i) {
     const K k = keyat(i);
     hs[i] = run;
@@ -259,42 +349,6 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
   }
   if (tid == 0) hs[ntot] = htot;
   __syncthreads();
-
-  // Unique count per row (long rows: from the long-row pass), then row scan.
-  int cnts[kRowsPerThread];
-  int csum = 0;
-#pragma unroll
-  for (int i = 0; i < kRowsPerThread; ++i) {
-    const int r = tid * kRowsPerThread + i;
-    int cnt = 0;
-    if (r < R) {
-      const int len = S.r_len[r];
-      cnt = len < 0 ? ucount[clo + r] : hs[S.r_start[r] + len] - hs[S.r_start[r]];
-    }
-    cnts[i] = cnt;
-    csum += cnt;
-  }
-  int ttot;
-  int cex = block_exclusive_scan<kTileThreads>(csum, S.scan, &ttot);
-  if (ttot != agg && tid == 0) record_error(st, CM_ERR_INVALID, ERR_SITE_BOUNDS);  // count paths disagree
-  if (tid < 32) {
-    const unsigned long long base = lookback_resolve(lb, tile, (unsigned long long)agg, st);
-    if (tid == 0) S.s_base = base;
-  }
-#pragma unroll
-  for (int i = 0; i < kRowsPerThread; ++i) {
-    const int r = tid * kRowsPerThread + i;
-    if (r < R) S.r_c[r] = cex;  // exclusive unique prefix of row r within the tile
-    cex += cnts[i];
-  }
-  __syncthreads();
-  const long long base = (long long)S.s_base;
-#pragma unroll
-  for (int i = 0; i < kRowsPerThread; ++i) {
-    const int r = tid * kRowsPerThread + i;
-    if (r < R) cxadj[clo + r + 1] = (int)(base + S.r_c[r] + cnts[i]);
-  }
-  if (tile == 0 && tid == 0) cxadj[0] = 0;
   for (int i = tid; i < ntot; i += kTileThreads) {
     const int hb = hs[i];
     if (hs[i + 1] == hb) continue;  // not a head
@@ -302,13 +356,9 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
     const int r = KT::row(k);
     unsigned sum = (unsigned)wat(i);
     for (int j = i + 1; j < ntot && keyat(j) == k; ++j) sum += (unsigned)wat(j);
-    const long long pos = base + S.r_c[r] + (hb - hs[S.r_start[r]]);
+    const long long pos = (long long)S.r_out[r] + (hb - hs[S.T.r_start[r]]);
     cadjncy[pos] = (int)KT::id(k);
     cadjwgt[pos] = (int)sum;
-  }
-  if (tid == 0 && (long long)tile * kTileDiag <= dend && dend < (long long)(tile + 1) * kTileDiag) {
-    d_sizes[0] = nc;
-    d_sizes[1] = (int)(base + ttot);
   }
 }
 
@@ -317,7 +367,7 @@ k_contract_tiles(const int *__restrict__ xadj, const int *__restrict__ adjncy, c
 // ---------------------------------------------------------------------------
 template <int CAP>
 struct RowSmem {
-  unsigned long long v[2][CAP + 8];  // packed (coarse id << 32 | weight); +8 for the sentinel hs[cnt]
+  unsigned long long v[2][padded_size(CAP + 8)];  // packed (coarse id << 32 | weight) at pad16(i); +8 for hs[cnt]
 };
 using ChunkSmem = RowSmem<kChunk>;
 
@@ -357,7 +407,7 @@ __device__ __forceinline__ void sort_row_segment(RowSmem<CAP> &S, int *scan, int
       const int t = t0 + u * NT;
       if (t < cnt) {
         const unsigned key = x[u] == c ? kSelfKey : (unsigned)x[u];
-        S.v[0][t] = ((unsigned long long)key << 32) | (unsigned)w[u];
+        S.v[0][pad16(t)] = ((unsigned long long)key << 32) | (unsigned)w[u];
       }
     }
   }
@@ -366,7 +416,7 @@ __device__ __forceinline__ void sort_row_segment(RowSmem<CAP> &S, int *scan, int
   const unsigned long long *P = S.v[b];
   if (!whole) {
     for (int t = threadIdx.x; t < cnt; t += NT) {
-      const unsigned long long e = P[t];
+      const unsigned long long e = P[pad16(t)];
       run_dst[t] = make_int2((int)(unsigned)(e >> 32), (int)(unsigned)e);
     }
   } else {
@@ -374,8 +424,8 @@ __device__ __forceinline__ void sort_row_segment(RowSmem<CAP> &S, int *scan, int
     const int ipt = (cnt + NT - 1) / NT;
     const int i0 = min(cnt, (int)threadIdx.x * ipt), i1 = min(cnt, i0 + ipt);
     auto head = [&](int i) {
-      const unsigned k = (unsigned)(P[i] >> 32);
-      return k != kSelfKey && (i == 0 || (unsigned)(P[i - 1] >> 32) != k);
+      const unsigned k = (unsigned)(P[pad16(i)] >> 32);
+      return k != kSelfKey && (i == 0 || (unsigned)(P[pad16(i - 1)] >> 32) != k);
     };
     int hc = 0;
     for (int i = i0; i < i1; ++i) hc += head(i);
@@ -389,9 +439,9 @@ __device__ __forceinline__ void sort_row_segment(RowSmem<CAP> &S, int *scan, int
     __syncthreads();
     for (int i = threadIdx.x; i < cnt; i += NT) {
       if (hs[i + 1] == hs[i]) continue;
-      const unsigned k = (unsigned)(P[i] >> 32);
-      unsigned sum = (unsigned)P[i];
-      for (int j = i + 1; j < cnt && (unsigned)(P[j] >> 32) == k; ++j) sum += (unsigned)P[j];
+      const unsigned k = (unsigned)(P[pad16(i)] >> 32);
+      unsigned sum = (unsigned)P[pad16(i)];
+      for (int j = i + 1; j < cnt && (unsigned)(P[pad16(j)] >> 32) == k; ++j) sum += (unsigned)P[pad16(j)];
       dedup_dst[hs[i]] = make_int2((int)k, (int)sum);
     }
   }
@@ -634,19 +684,24 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   DevStatus *st = ctx->d_status;
   cudaMemsetAsync(ctr, 0, 64, s);
   cudaMemsetAsync(&st->max_row, 0, sizeof(int), s);
-  cudaMemsetAsync(lb, 0, (size_t)(ntiles + 1) * 8, s);
+  cudaMemsetAsync(lb, 0, (size_t)(n / (kScanThreads * kScanItems) + 3) * 8, s);
   int rc = launch_cmap(ctx, (int32_t)n, fine->xadj, fine->vwgt, match, cmap, leader, coarse->vwgt, eoff,
                        d_sizes /* n' lands in d_sizes[0] */, long_list, kLongThr, kChunk, ctr, chunk_row, first_row,
                        kTileDiag, mid_list, mid_ctr, (int32_t)mid_cap, row_meta, s);
   if (rc) return rc;
   const int sms = ctx->num_sms;
   const bool small_ids = n < kSmallIdLimit;
-  const size_t tile_smem = small_ids ? sizeof(TileSmem<unsigned>) : sizeof(TileSmem<unsigned long long>);
-  if (small_ids)
-    cudaFuncSetAttribute(k_contract_tiles<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem);
-  else
-    cudaFuncSetAttribute(k_contract_tiles<unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)tile_smem);
+  const size_t count_smem = small_ids ? sizeof(CountSmem<unsigned>) : sizeof(CountSmem<unsigned long long>);
+  const size_t emit_smem = small_ids ? sizeof(EmitSmem<unsigned>) : sizeof(EmitSmem<unsigned long long>);
+  if (small_ids) {
+    cudaFuncSetAttribute(k_tile_count<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)count_smem);
+    cudaFuncSetAttribute(k_tile_emit<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)emit_smem);
+  } else {
+    cudaFuncSetAttribute(k_tile_count<unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)count_smem);
+    cudaFuncSetAttribute(k_tile_emit<unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)emit_smem);
+  }
   cudaFuncSetAttribute(k_mid_sort<256, 2 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(RowSmem<2 * kLongThr>));
   cudaFuncSetAttribute(k_mid_sort<512, 4 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -655,9 +710,10 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
                        (int)sizeof(RowSmem<kChunk>));
   cudaFuncSetAttribute(k_long_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem));
 
-  // Long rows: the three size classes run on the auxiliary streams while the
-  // chunked rows are sorted, merged and deduplicated on the caller's stream;
-  // the tiles wait for all of them (they need every long row's unique count).
+  // Pass 1.  Long rows on the auxiliary streams (three size classes; the
+  // chunked rows' sort, merge passes and dedup after the largest class) while
+  // the tiles count the short rows' unique entries on the caller's stream.
+  // Both write ucount; the scan waits for all of them.
   stage_begin(ctx, s);
   cudaEventRecord(ctx->fork_ev, s);
   for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(ctx->aux[i], ctx->fork_ev, 0);
@@ -670,11 +726,9 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   k_mid_sort<1024, kChunk><<<sms, 1024, sizeof(RowSmem<kChunk>), ctx->aux[2]>>>(
       fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, row_meta, mid_list + 2 * mid_cap,
       mid_ctr + 2, stage1, ucount);
-  ctx->launches += 3;
-  for (int i = 0; i < 3; ++i) cudaEventRecord(ctx->join_ev[i], ctx->aux[i]);
-  k_long_sort<<<sms, kChunkThreads, sizeof(ChunkSmem), s>>>(fine->xadj, fine->adjncy, fine->adjwgt, match, cmap,
-                                                           leader, eoff, row_meta, long_list, chunk_row, ctr, stage0);
-  ctx->launches++;
+  k_long_sort<<<sms, kChunkThreads, sizeof(ChunkSmem), ctx->aux[2]>>>(
+      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, row_meta, long_list, chunk_row, ctr, stage0);
+  ctx->launches += 4;
   {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_long_merge, kMergeThreads, 0);
@@ -686,32 +740,51 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
     int2 *a4 = stage0, *a5 = stage1;
     DevStatus *a6 = st;
     void *args[] = {(void *)&a0, (void *)&a1, (void *)&a2, (void *)&a3, (void *)&a4, (void *)&a5, (void *)&a6};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_long_merge, dim3(grid), dim3(kMergeThreads), args, 0, s);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_long_merge, dim3(grid), dim3(kMergeThreads), args, 0,
+                                                ctx->aux[2]);
     if (e != cudaSuccess) return cuda_status(e, "contract: long-row merge launch");
     ctx->launches++;
   }
-  k_long_dedup<<<sms * 2, kDedupThreads, 0, s>>>(long_list, eoff, ctr, stage0, stage1, ucount);
+  k_long_dedup<<<sms * 2, kDedupThreads, 0, ctx->aux[2]>>>(long_list, eoff, ctr, stage0, stage1, ucount);
+  ctx->launches++;
+  for (int i = 0; i < 3; ++i) cudaEventRecord(ctx->join_ev[i], ctx->aux[i]);
+  // d_sizes[0] holds n' (written by the cmap scan).
+  if (small_ids)
+    k_tile_count<unsigned><<<(unsigned)ntiles, kTileThreads, count_smem, s>>>(
+        fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, ucount, st);
+  else
+    k_tile_count<unsigned long long><<<(unsigned)ntiles, kTileThreads, count_smem, s>>>(
+        fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, ucount, st);
   ctx->launches++;
   for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(s, ctx->join_ev[i], 0);
-  stage_end(ctx, CM_STAGE_LONG_SORT, s);
+  stage_end(ctx, CM_STAGE_TILE_COUNT, s);
 
-  // d_sizes[0] holds n' (written by the cmap scan).
+  // cxadj = exclusive scan of ucount; d_sizes[1] = m'.
   stage_begin(ctx, s);
+  const int64_t scan_tiles = (n + kScanThreads * kScanItems - 1) / (kScanThreads * kScanItems);
+  k_count_scan<<<(unsigned)scan_tiles, kScanThreads, 0, s>>>(ucount, d_sizes, coarse->xadj, d_sizes, lb, st);
+  ctx->launches++;
+  stage_end(ctx, CM_STAGE_SCAN, s);
+
+  // Pass 2.  Tiles sort, merge and write the short rows; the long rows'
+  // unique entries are copied out on an auxiliary stream meanwhile.
+  stage_begin(ctx, s);
+  cudaEventRecord(ctx->fork_ev, s);
+  cudaStreamWaitEvent(ctx->aux[0], ctx->fork_ev, 0);
+  k_long_copy<<<sms * 4, 256, 0, ctx->aux[0]>>>(long_list, chunk_row, eoff, ctr, mid_list, mid_ctr, (int)mid_cap,
+                                                 stage0, stage1, ucount, coarse->xadj, coarse->adjncy, coarse->adjwgt);
+  cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
   if (small_ids)
-    k_contract_tiles<unsigned><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
-        fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, d_sizes, first_row, row_meta, ucount, lb,
-        coarse->xadj, coarse->adjncy, coarse->adjwgt, d_sizes, st);
+    k_tile_emit<unsigned><<<(unsigned)ntiles, kTileThreads, emit_smem, s>>>(
+        fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, coarse->xadj, coarse->adjncy,
+        coarse->adjwgt, st);
   else
-    k_contract_tiles<unsigned long long><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
-        fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, d_sizes, first_row, row_meta, ucount, lb,
-        coarse->xadj, coarse->adjncy, coarse->adjwgt, d_sizes, st);
-  stage_end(ctx, CM_STAGE_TILES, s);
-  ctx->launches++;
-  stage_begin(ctx, s);
-  k_long_copy<<<sms * 4, 256, 0, s>>>(long_list, chunk_row, eoff, ctr, mid_list, mid_ctr, (int)mid_cap, stage0,
-                                       stage1, ucount, coarse->xadj, coarse->adjncy, coarse->adjwgt);
-  stage_end(ctx, CM_STAGE_LONG_COPY, s);
-  ctx->launches++;
+    k_tile_emit<unsigned long long><<<(unsigned)ntiles, kTileThreads, emit_smem, s>>>(
+        fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, coarse->xadj, coarse->adjncy,
+        coarse->adjwgt, st);
+  ctx->launches += 2;
+  cudaStreamWaitEvent(s, ctx->join_ev[0], 0);
+  stage_end(ctx, CM_STAGE_TILE_EMIT, s);
   return check_launch(ctx, "contract");
 }
 

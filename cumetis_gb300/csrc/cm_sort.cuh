@@ -104,21 +104,27 @@ __device__ int block_merge_sort(K *k0, int *w0, K *k1, int *w1, int n, K pad) {
 
 namespace cm {
 
+// Padded shared-memory index for 64-bit words: one spare word every 16, so
+// that a warp whose lanes touch consecutive runs of 4 or 8 words (stride 32 or
+// 64 bytes) spreads over all banks instead of colliding 8- or 16-fold.
+__host__ __device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int padded_size(int n) { return n + (n >> 4) + 1; }
+
 // Block merge sort of packed 64-bit words (sort key in the high bits, payload
-// in the low bits; ties among equal keys may end in any order).  One word per
-// entry halves the shared-memory traffic of the key/payload version, and the
-// merge keeps both run heads in registers so each output costs one load.
-// Returns 0 if the result is in a, 1 if in b.  All NT threads must call it.
+// in the low bits; ties among equal keys may end in any order), stored at
+// padded indices pad16(i).  a and b hold padded_size(n rounded up to E)
+// words.  Returns 0 if the result is in a, 1 if in b.  All NT threads must
+// call it.
 template <int NT, int E>
 __device__ int block_merge_sort_packed(unsigned long long *a, unsigned long long *b, int n) {
   const int npad = ((n + E - 1) / E) * E;
-  for (int i = n + (int)threadIdx.x; i < npad; i += NT) a[i] = ~0ull;
+  for (int i = n + (int)threadIdx.x; i < npad; i += NT) a[pad16(i)] = ~0ull;
   __syncthreads();
   const int nruns = npad / E;
   for (int q = threadIdx.x; q < nruns; q += NT) {
     unsigned long long v[E];
 #pragma unroll
-    for (int i = 0; i < E; ++i) v[i] = a[q * E + i];
+    for (int i = 0; i < E; ++i) v[i] = a[pad16(q * E + i)];
 #pragma unroll
     for (int size = 2; size <= E; size <<= 1) {
 #pragma unroll
@@ -134,7 +140,7 @@ __device__ int block_merge_sort_packed(unsigned long long *a, unsigned long long
       }
     }
 #pragma unroll
-    for (int i = 0; i < E; ++i) a[q * E + i] = v[i];
+    for (int i = 0; i < E; ++i) a[pad16(q * E + i)] = v[i];
   }
   __syncthreads();
   unsigned long long *src = a, *dst = b;
@@ -145,22 +151,32 @@ __device__ int block_merge_sort_packed(unsigned long long *a, unsigned long long
       const int ps = (out / (2 * width)) * (2 * width);
       const int alen = min(width, npad - ps);
       const int blen = min(width, npad - ps - alen);
-      const unsigned long long *A = src + ps;
-      const unsigned long long *B = A + alen;
+      const int bs = ps + alen;  // B starts here
       const int diag = out - ps;
       int i;
-      if (blen == 0) i = diag;
-      else if (A[alen - 1] <= B[0]) i = diag < alen ? diag : alen;
-      else i = merge_path(A, alen, B, blen, diag);
+      if (blen == 0) {
+        i = diag;
+      } else if (src[pad16(ps + alen - 1)] <= src[pad16(bs)]) {
+        i = diag < alen ? diag : alen;
+      } else {
+        int lo = diag > blen ? diag - blen : 0;
+        int hi = diag < alen ? diag : alen;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (src[pad16(ps + mid)] <= src[pad16(bs + diag - 1 - mid)]) lo = mid + 1;
+          else hi = mid;
+        }
+        i = lo;
+      }
       int j = diag - i;
-      unsigned long long ka = i < alen ? A[i] : ~0ull;
-      unsigned long long kb = j < blen ? B[j] : ~0ull;
+      unsigned long long ka = i < alen ? src[pad16(ps + i)] : ~0ull;
+      unsigned long long kb = j < blen ? src[pad16(bs + j)] : ~0ull;
 #pragma unroll
       for (int t = 0; t < E; ++t) {
         const bool takeA = (j >= blen) || (i < alen && ka <= kb);
-        dst[out + t] = takeA ? ka : kb;
-        if (takeA) { ++i; ka = i < alen ? A[i] : ~0ull; }
-        else { ++j; kb = j < blen ? B[j] : ~0ull; }
+        dst[pad16(out + t)] = takeA ? ka : kb;
+        if (takeA) { ++i; ka = i < alen ? src[pad16(ps + i)] : ~0ull; }
+        else { ++j; kb = j < blen ? src[pad16(bs + j)] : ~0ull; }
       }
     }
     __syncthreads();
