@@ -45,22 +45,18 @@ constexpr int kChunk = 8192;                      // long-row chunk (entries sor
 constexpr int kChunkThreads = 1024;
 constexpr unsigned kSelfKey = 0xffffffffu;        // self loops sort last in their row
 
-// Composite sort key (tile-local row, coarse id).  32-bit when coarse ids fit
-// in 23 bits (n < 2^23 - 1; rows need 9 bits for kTileDiag = 512), else 64-bit.  The self-loop id is the largest
-// id value, so self loops sort last in their row; the pad sorts after all.
+// Composite key (tile-local row, coarse id).  32-bit when coarse ids fit in
+// 23 bits (n < 2^23 - 1; rows need 9 bits for kTileDiag = 512), else 64-bit.
+// All-ones is the empty hash slot and the sort pad; no key reaches it.
 template <typename K> struct KeyT;
 template <> struct KeyT<unsigned> {
   static constexpr int kShift = 23;
   static constexpr unsigned kIdMask = (1u << 23) - 1;
-  static constexpr unsigned kSelf = kIdMask;
-  static constexpr unsigned kPad = 0xffffffffu;
   static __device__ __forceinline__ unsigned make(int r, unsigned id) { return ((unsigned)r << kShift) | id; }
   static __device__ __forceinline__ int row(unsigned k) { return (int)(k >> kShift); }
   static __device__ __forceinline__ unsigned id(unsigned k) { return k & kIdMask; }
 };
 template <> struct KeyT<unsigned long long> {
-  static constexpr unsigned kSelf = 0xffffffffu;
-  static constexpr unsigned long long kPad = ~0ull;
   static __device__ __forceinline__ unsigned long long make(int r, unsigned id) {
     return ((unsigned long long)r << 32) | id;
   }
@@ -85,17 +81,104 @@ __device__ __forceinline__ int upper_bound_smem(const int *a, int n, int x) {
 // (as find_cnvtxsedge_original places them, cuMetis.cu:1014-1020).
 __device__ __forceinline__ int expanded_src(int o, int xl, int dl, int xf) { return o < dl ? xl + o : xf + (o - dl); }
 
-// Per-tile row table shared by the count and emit passes.
+// ---------------------------------------------------------------------------
+// Shared-memory hash set with weight sums (one per tile or per row).  Keys are
+// inserted with atomicCAS into open-addressed slots (linear probing, Fibonacci
+// hashing); the weight of every copy of a key is added to its slot.  A slot,
+// once set, never changes, so a plain read that finds the key is final.
+// ---------------------------------------------------------------------------
+template <typename K>
+__device__ __forceinline__ unsigned hash_home(K key, int shift) {
+  return (unsigned)(((unsigned long long)key * 0x9E3779B97F4A7C15ull) >> shift);
+}
+
+template <typename K>
+__device__ __forceinline__ void hash_add(K *hk, int *hw, unsigned hmask, int shift, K key, int w) {
+  const K empty = ~(K)0;
+  unsigned h = hash_home(key, shift);
+  for (unsigned p = 0; p <= hmask; ++p) {
+    K old = hk[h];
+    if (old == empty) old = atomicCAS(&hk[h], empty, key);
+    if (old == empty || old == key) {
+      atomicAdd(&hw[h], w);
+      return;
+    }
+    h = (h + 1) & hmask;
+  }
+}
+
+// Weight sum of a key known to be in the set.
+template <typename K>
+__device__ __forceinline__ int hash_get(const K *hk, const int *hw, unsigned hmask, int shift, K key) {
+  unsigned h = hash_home(key, shift);
+  for (unsigned p = 0; p <= hmask; ++p) {
+    if (hk[h] == key) return hw[h];
+    h = (h + 1) & hmask;
+  }
+  return 0;
+}
+
+// Table size for n keys: the power of two >= 2n (at least 64, at most cap);
+// returns log2 of it.
+__device__ __forceinline__ int hash_log2(int n, int cap_log2) {
+  int lg = 6;
+  while (lg < cap_log2 && (1 << lg) < 2 * n) ++lg;
+  return lg;
+}
+
+// Appends the set's keys to dst (arbitrary order, warp-aggregated); returns
+// their number.  All NT threads call it; *ctr is a shared counter set to 0.
+template <typename K, int NT>
+__device__ __forceinline__ int hash_compact(const K *hk, int hsize, K *dst, int *ctr) {
+  const K empty = ~(K)0;
+  const int lane = threadIdx.x & 31;
+  for (int i0 = threadIdx.x - lane; i0 < hsize; i0 += NT) {
+    const int i = i0 + lane;
+    const K k = i < hsize ? hk[i] : empty;
+    const unsigned m = __ballot_sync(0xffffffffu, k != empty);
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(ctr, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (k != empty) dst[padk<K>(base + __popc(m & ((1u << lane) - 1)))] = k;
+  }
+  __syncthreads();
+  const int n = *ctr;
+  __syncthreads();
+  return n;
+}
+
+// ---------------------------------------------------------------------------
+// Contraction tiles
+// ---------------------------------------------------------------------------
+constexpr int kTileHashLog2 = 11;                 // 2048 slots (> kTileCap, load <= 3/4)
+constexpr int kTileHash = 1 << kTileHashLog2;
+static_assert(kTileHash > kTileCap, "tile hash must have a free slot for every entry");
+
 struct TileRows {
-  int r_xl[kTileDiag], r_dl[kTileDiag], r_xf[kTileDiag], r_start[kTileDiag], r_len[kTileDiag];
+  int r_xl[kTileDiag], r_dl[kTileDiag], r_xf[kTileDiag], r_start[kTileDiag];
+};
+
+template <typename K>
+struct TileSmem {
+  union {
+    TileRows T;                                   // gather
+    K keys[2][padded_k<K>(kTileCap + 8)];         // sort of the unique keys
+  } u;
+  K hk[kTileHash];
+  int hw[kTileHash];
+  int r_out[kTileDiag];                           // staging offset eoff[c] of a short row, -1 for a long row
+  int ustart[kTileDiag + 1];                      // first sorted unique key of each row
   int scan[kTileThreads / 32 + 1];
+  int ctr;
 };
 
 // Rows [clo, clo+R) of tile t (rows whose diagonal c + eoff[c] lies in
 // [tD, (t+1)D)); loads their metadata and lays the short rows' entries out
 // back to back (long rows take no space).  Returns the number of entries.
-__device__ __forceinline__ int tile_rows(TileRows &T, int tile, int nc, long long dend, const int *first_row,
-                                         const int4 *row_meta, int &clo, int &R, DevStatus *st) {
+template <typename K>
+__device__ __forceinline__ int tile_rows(TileSmem<K> &S, int tile, int nc, long long dend,
+                                         const int *__restrict__ first_row, const int4 *__restrict__ row_meta,
+                                         const int *__restrict__ eoff, int &clo, int &R, DevStatus *st) {
   const int tid = threadIdx.x;
   const long long last = dend / kTileDiag;
   clo = tile <= last ? first_row[tile] : nc;
@@ -114,17 +197,18 @@ __device__ __forceinline__ int tile_rows(TileRows &T, int tile, int nc, long lon
     int len = 0;
     if (r < R) {
       const int4 md = row_meta[clo + r];  // (leader start, leader length, follower start, length)
-      T.r_xl[r] = md.x;
-      T.r_dl[r] = md.y;
-      T.r_xf[r] = md.z;
-      T.r_len[r] = md.w > kLongThr ? -1 : md.w;
-      len = md.w > kLongThr ? 0 : md.w;
+      S.u.T.r_xl[r] = md.x;
+      S.u.T.r_dl[r] = md.y;
+      S.u.T.r_xf[r] = md.z;
+      const bool lng = md.w > kLongThr;
+      S.r_out[r] = lng ? -1 : eoff[clo + r];
+      len = lng ? 0 : md.w;
     }
     lens[i] = len;
     mysum += len;
   }
   int ntot;
-  int ex = block_exclusive_scan<kTileThreads>(mysum, T.scan, &ntot);
+  int ex = block_exclusive_scan<kTileThreads>(mysum, S.scan, &ntot);
   const bool overflow = ntot > kTileCap;
   if (overflow) {
     if (tid == 0) record_error(st, CM_ERR_INVALID, ERR_SITE_BOUNDS);
@@ -133,92 +217,93 @@ __device__ __forceinline__ int tile_rows(TileRows &T, int tile, int nc, long lon
 #pragma unroll
   for (int i = 0; i < kRowsPerThread; ++i) {
     const int r = tid * kRowsPerThread + i;
-    if (r < R) T.r_start[r] = overflow ? 0 : ex;
-    if (r < R && overflow) T.r_len[r] = 0;
+    if (r < R) {
+      S.u.T.r_start[r] = overflow ? 0 : ex;
+      if (overflow) S.r_out[r] = -1;
+    }
     ex += lens[i];
   }
   __syncthreads();
   return ntot;
 }
 
-// Gathers 4 entries per thread per step: row, coarse id (self loops marked)
-// and weight of expanded entries e0 + u*kTileThreads; consecutive entries of a
-// fine row go to consecutive lanes (coalesced adjncy/adjwgt reads).
-__device__ __forceinline__ void tile_gather4(const TileRows &T, int R, int clo, int ntot, int e0,
-                                             const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
-                                             const int *__restrict__ cmap, int (&rr)[4], int (&id)[4], int (&w)[4],
-                                             unsigned selfkey) {
-  int src[4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    const int e = e0 + u * kTileThreads;
-    rr[u] = 0;
-    src[u] = -1;
-    if (e < ntot) {
-      const int r = upper_bound_smem(T.r_start, R, e) - 1;
-      rr[u] = r;
-      src[u] = expanded_src(e - T.r_start[r], T.r_xl[r], T.r_dl[r], T.r_xf[r]);
-    }
-  }
-#pragma unroll
-  for (int u = 0; u < 4; ++u) {
-    id[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
-    w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
-  }
-#pragma unroll
-  for (int u = 0; u < 4; ++u) id[u] = src[u] >= 0 ? cmap[id[u]] : 0;
-#pragma unroll
-  for (int u = 0; u < 4; ++u)
-    if (src[u] >= 0 && id[u] == clo + rr[u]) id[u] = (int)selfkey;
-}
-
-// Pass 1: unique coarse ids per short row, counted with a shared-memory hash
-// set of (row, id) keys; writes ucount[c].  No sort, no look-back.
-template <typename K>
-struct CountSmem {
-  TileRows T;
-  K tab[kHashCap];
-  int cnt[kTileDiag];
-};
-
+// One pass per tile: gathers the short rows' expanded entries (row, coarse
+// id, weight), merges duplicates in a shared-memory hash set (self loops are
+// dropped), sorts the unique (row, id) keys, and writes each row's unique
+// entries, ascending by id with summed weights, to stage[eoff[c] ...) and
+// their number to ucount[c].
 template <typename K>
 __global__ void __launch_bounds__(kTileThreads)
-k_tile_count(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
-             const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
-             const int4 *__restrict__ row_meta, int *__restrict__ ucount, DevStatus *st) {
+k_contract_tiles(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
+                 const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
+                 const int4 *__restrict__ row_meta, int2 *__restrict__ stage, int *__restrict__ ucount,
+                 DevStatus *st) {
   using KT = KeyT<K>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  CountSmem<K> &S = *reinterpret_cast<CountSmem<K> *>(smem_raw);
+  TileSmem<K> &S = *reinterpret_cast<TileSmem<K> *>(smem_raw);
   const int tid = threadIdx.x;
   const int nc = *d_cn;
   const long long dend = (long long)nc + eoff[nc];
   int clo, R;
-  const int ntot = tile_rows(S.T, blockIdx.x, nc, dend, first_row, row_meta, clo, R, st);
-  unsigned hsize = 64;
-  while (hsize < (unsigned)(2 * ntot)) hsize <<= 1;  // <= kHashCap since ntot <= kTileCap
+  if (tid == 0) S.ctr = 0;
+  const int ntot = tile_rows(S, blockIdx.x, nc, dend, first_row, row_meta, eoff, clo, R, st);
+  const int lg = hash_log2(ntot, kTileHashLog2);
+  const int hsize = 1 << lg, shift = 64 - lg;
   const unsigned hmask = hsize - 1;
-  for (int i = tid; i < (int)hsize; i += kTileThreads) S.tab[i] = KT::kPad;
-  for (int r = tid; r < R; r += kTileThreads) S.cnt[r] = 0;
+  for (int i = tid; i < hsize; i += kTileThreads) {
+    S.hk[i] = ~(K)0;
+    S.hw[i] = 0;
+  }
   __syncthreads();
   for (int e0 = tid; e0 < ntot; e0 += 4 * kTileThreads) {
-    int rr[4], id[4], w[4];
-    tile_gather4(S.T, R, clo, ntot, e0, adjncy, adjwgt, cmap, rr, id, w, KT::kSelf);
+    int src[4], rr[4], id[4], w[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      if (e0 + u * kTileThreads >= ntot || (unsigned)id[u] == KT::kSelf) continue;
-      const K key = KT::make(rr[u], (unsigned)id[u]);
-      unsigned h = (unsigned)(((unsigned long long)key * 0x9E3779B97F4A7C15ull) >> 40) & hmask;
-      for (unsigned probe = 0; probe < hsize; ++probe) {
-        const K old = atomicCAS(&S.tab[h], KT::kPad, key);
-        if (old == KT::kPad) { atomicAdd(&S.cnt[rr[u]], 1); break; }
-        if (old == key) break;
-        h = (h + 1) & hmask;
+      const int e = e0 + u * kTileThreads;
+      rr[u] = 0;
+      src[u] = -1;
+      if (e < ntot) {
+        const int r = upper_bound_smem(S.u.T.r_start, R, e) - 1;
+        rr[u] = r;
+        src[u] = expanded_src(e - S.u.T.r_start[r], S.u.T.r_xl[r], S.u.T.r_dl[r], S.u.T.r_xf[r]);
       }
     }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      id[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
+      w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) id[u] = src[u] >= 0 ? cmap[id[u]] : 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (src[u] >= 0 && id[u] != clo + rr[u])
+        hash_add<K>(S.hk, S.hw, hmask, shift, KT::make(rr[u], (unsigned)id[u]), w[u]);
+  }
+  __syncthreads();  // gather done: the row table is dead, its space holds the keys
+  const int U = hash_compact<K, kTileThreads>(S.hk, hsize, S.u.keys[0], &S.ctr);
+  const int b = block_sort_keys<K, kTileThreads, kTileE>(S.u.keys[0], S.u.keys[1], U);
+  const K *sk = S.u.keys[b];
+  // first sorted key of each row: lower bound of (r, 0)
+  for (int r = tid; r <= R; r += kTileThreads) {
+    const K key = r < R ? KT::make(r, 0u) : ~(K)0;
+    int lo = 0, hi = U;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (sk[padk<K>(mid)] < key) lo = mid + 1;
+      else hi = mid;
+    }
+    S.ustart[r] = r < R ? lo : U;
   }
   __syncthreads();
   for (int r = tid; r < R; r += kTileThreads)
-    if (S.T.r_len[r] >= 0) ucount[clo + r] = S.cnt[r];
+    if (S.r_out[r] >= 0) ucount[clo + r] = S.ustart[r + 1] - S.ustart[r];
+  for (int i = tid; i < U; i += kTileThreads) {
+    const K k = sk[padk<K>(i)];
+    const int r = KT::row(k);
+    const int w = hash_get<K>(S.hk, S.hw, hmask, shift, k);
+    stage[S.r_out[r] + (i - S.ustart[r])] = make_int2((int)KT::id(k), w);
+  }
 }
 
 // Exclusive scan of the per-row unique counts into cxadj (decoupled look-back
@@ -266,99 +351,52 @@ k_count_scan(const int *__restrict__ ucount, const int *d_cn, int *__restrict__ 
   }
 }
 
-// Pass 2: gathers each tile's entries again, sorts them by (row, coarse id),
-// merges duplicates and writes every unique entry to its final place
-// cxadj[row] + rank.
-template <typename K>
-struct EmitSmem;
-template <>
-struct EmitSmem<unsigned> {  // packed (row:9 | id:23) << 32 | weight, padded layout
-  TileRows T;
-  int r_out[kTileDiag];
-  unsigned long long p[2][padded_size(kTileCap + 8)];
-};
-template <>
-struct EmitSmem<unsigned long long> {  // 64-bit (row, id) keys with separate weights
-  TileRows T;
-  int r_out[kTileDiag];
-  unsigned long long k[2][kTileCap];
-  int w[2][kTileCap];
-};
-
-template <typename K>
+// Copies the short rows' unique entries from the stage to their final place
+// cxadj[c] (one block per tile, one thread per entry).
 __global__ void __launch_bounds__(kTileThreads)
-k_tile_emit(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
-            const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
-            const int4 *__restrict__ row_meta, const int *__restrict__ cxadj, int *__restrict__ cadjncy,
-            int *__restrict__ cadjwgt, DevStatus *st) {
-  using KT = KeyT<K>;
-  constexpr bool kPacked = sizeof(K) == 4;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  EmitSmem<K> &S = *reinterpret_cast<EmitSmem<K> *>(smem_raw);
+k_copy_tiles(const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
+             const int *__restrict__ ucount, const int *__restrict__ cxadj, const int2 *__restrict__ stage,
+             int *__restrict__ cadjncy, int *__restrict__ cadjwgt) {
+  __shared__ int s_pre[kTileDiag + 1], s_src[kTileDiag], s_dst[kTileDiag], s_scan[kTileThreads / 32 + 1];
   const int tid = threadIdx.x;
   const int nc = *d_cn;
   const long long dend = (long long)nc + eoff[nc];
-  int clo, R;
-  const int ntot = tile_rows(S.T, blockIdx.x, nc, dend, first_row, row_meta, clo, R, st);
-  for (int r = tid; r < R; r += kTileThreads) S.r_out[r] = cxadj[clo + r];
-  for (int e0 = tid; e0 < ntot; e0 += 4 * kTileThreads) {
-    int rr[4], id[4], w[4];
-    tile_gather4(S.T, R, clo, ntot, e0, adjncy, adjwgt, cmap, rr, id, w, KT::kSelf);
+  const long long last = dend / kTileDiag;
+  const int tile = blockIdx.x;
+  const int clo = tile <= last ? first_row[tile] : nc;
+  const int chi = tile + 1 <= last ? first_row[tile + 1] : nc;
+  const int R = max(0, min(kTileDiag, chi - clo));
+  constexpr int kRowsPerThread = kTileDiag / kTileThreads;
+  int cnt[kRowsPerThread];
+  int mysum = 0;
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int e = e0 + u * kTileThreads;
-      if (e >= ntot) continue;
-      if constexpr (kPacked) {
-        S.p[0][pad16(e)] = ((unsigned long long)KT::make(rr[u], (unsigned)id[u]) << 32) | (unsigned)w[u];
-      } else {
-        S.k[0][e] = KT::make(rr[u], (unsigned)id[u]);
-        S.w[0][e] = w[u];
-      }
+  for (int i = 0; i < kRowsPerThread; ++i) {
+    const int r = tid * kRowsPerThread + i;
+    cnt[i] = 0;
+    if (r < R) {
+      const int c = clo + r;
+      const int e0 = eoff[c];
+      if (eoff[c + 1] - e0 <= kLongThr) cnt[i] = ucount[c];
+      s_src[r] = e0;
+      s_dst[r] = cxadj[c];
     }
+    mysum += cnt[i];
+  }
+  int U;
+  int ex = block_exclusive_scan<kTileThreads>(mysum, s_scan, &U);
+#pragma unroll
+  for (int i = 0; i < kRowsPerThread; ++i) {
+    const int r = tid * kRowsPerThread + i;
+    if (r < R) s_pre[r] = ex;
+    ex += cnt[i];
   }
   __syncthreads();
-  int b;
-  if constexpr (kPacked) b = block_merge_sort_packed<kTileThreads, kTileE>(S.p[0], S.p[1], ntot);
-  else b = block_merge_sort<K, kTileThreads, kTileE>(S.k[0], S.w[0], S.k[1], S.w[1], ntot, KT::kPad);
-  auto keyat = [&](int i) -> K {
-    if constexpr (kPacked) return (K)(S.p[b][pad16(i)] >> 32);
-    else return S.k[b][i];
-  };
-  auto wat = [&](int i) -> int {
-    if constexpr (kPacked) return (int)(unsigned)S.p[b][pad16(i)];
-    else return S.w[b][i];
-  };
-  int *hs;
-  if constexpr (kPacked) hs = reinterpret_cast<int *>(S.p[b ^ 1]);
-  else hs = reinterpret_cast<int *>(S.k[b ^ 1]);
-  // heads (first of a run of equal (row, id), not a self loop), one block scan
-  // over per-thread contiguous chunks
-  const int ipt = (ntot + kTileThreads - 1) / kTileThreads;
-  const int i0 = min(ntot, tid * ipt), i1 = min(ntot, i0 + ipt);
-  int hcnt = 0;
-  for (int i = i0; i < i1; ++i) {
-    const K k = keyat(i);
-    hcnt += (KT::id(k) != KT::kSelf) && (i == 0 || keyat(i - 1) != k);
-  }
-  int htot;
-  int run = block_exclusive_scan<kTileThreads>(hcnt, S.T.scan, &htot);
-  for (int i = i0; i < i1; ++i) {
-    const K k = keyat(i);
-    hs[i] = run;
-    run += (KT::id(k) != KT::kSelf) && (i == 0 || keyat(i - 1) != k);
-  }
-  if (tid == 0) hs[ntot] = htot;
-  __syncthreads();
-  for (int i = tid; i < ntot; i += kTileThreads) {
-    const int hb = hs[i];
-    if (hs[i + 1] == hb) continue;  // not a head
-    const K k = keyat(i);
-    const int r = KT::row(k);
-    unsigned sum = (unsigned)wat(i);
-    for (int j = i + 1; j < ntot && keyat(j) == k; ++j) sum += (unsigned)wat(j);
-    const long long pos = (long long)S.r_out[r] + (hb - hs[S.T.r_start[r]]);
-    cadjncy[pos] = (int)KT::id(k);
-    cadjwgt[pos] = (int)sum;
+  for (int o = tid; o < U; o += kTileThreads) {
+    const int r = upper_bound_smem(s_pre, R, o) - 1;
+    const int k = o - s_pre[r];
+    const int2 e = stage[s_src[r] + k];
+    cadjncy[s_dst[r] + k] = e.x;
+    cadjwgt[s_dst[r] + k] = e.y;
   }
 }
 
@@ -449,22 +487,70 @@ __device__ __forceinline__ void sort_row_segment(RowSmem<CAP> &S, int *scan, int
 }
 
 // Rows too long for a tile but <= kChunk entries, one size class per launch:
-// one block sorts and deduplicates one whole row (unique entries to stage1).
+// one block merges one whole row's duplicates in a shared-memory hash set,
+// sorts the unique coarse ids and writes them with their summed weights to
+// stage[eoff[c] ...); ucount[c] = unique entries.
+template <int CAP>
+struct MidSmem {
+  unsigned keys[2][padded_k<unsigned>(CAP + 8)];
+  unsigned hk[2 * CAP];
+  int hw[2 * CAP];
+  int ctr;
+};
+
+__host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v >> 1); }
+
 template <int NT, int CAP>
 __global__ void __launch_bounds__(NT)
-k_mid_sort(const int *__restrict__ xadj, const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
-           const int *__restrict__ match, const int *__restrict__ cmap, const int *__restrict__ leader,
+k_mid_rows(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
            const int *__restrict__ eoff, const int4 *__restrict__ row_meta, const int *__restrict__ list,
-           const int *__restrict__ count, int2 *__restrict__ stage1, int *__restrict__ ucount) {
+           const int *__restrict__ count, int2 *__restrict__ stage, int *__restrict__ ucount) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  RowSmem<CAP> &S = *reinterpret_cast<RowSmem<CAP> *>(smem_raw);
-  __shared__ int scan[NT / 32 + 1];
+  MidSmem<CAP> &S = *reinterpret_cast<MidSmem<CAP> *>(smem_raw);
+  constexpr int kLg = ilog2(2 * CAP);
   const int nrows = *count;
   for (int i = blockIdx.x; i < nrows; i += gridDim.x) {
     const int c = list[i];
     const int4 md = row_meta[c];
-    sort_row_segment<NT, CAP>(S, scan, c, md.x, md.y, md.z, 0, md.w, true, nullptr, stage1 + eoff[c], ucount + c,
-                              adjncy, adjwgt, cmap);
+    const int L = min(md.w, CAP);
+    const int lg = hash_log2(L, kLg);
+    const int hsize = 1 << lg, shift = 64 - lg;
+    const unsigned hmask = hsize - 1;
+    if (threadIdx.x == 0) S.ctr = 0;
+    for (int t = threadIdx.x; t < hsize; t += NT) {
+      S.hk[t] = ~0u;
+      S.hw[t] = 0;
+    }
+    __syncthreads();
+    for (int t0 = threadIdx.x; t0 < L; t0 += 4 * NT) {
+      int src[4], x[4], w[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int t = t0 + u * NT;
+        src[u] = t < L ? expanded_src(t, md.x, md.y, md.z) : -1;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        x[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
+        w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (src[u] >= 0 && x[u] != c) hash_add<unsigned>(S.hk, S.hw, hmask, shift, (unsigned)x[u], w[u]);
+    }
+    __syncthreads();
+    const int U = hash_compact<unsigned, NT>(S.hk, hsize, S.keys[0], &S.ctr);
+    const int b = block_sort_keys<unsigned, NT, 8>(S.keys[0], S.keys[1], U);
+    const unsigned *sk = S.keys[b];
+    int2 *dst = stage + eoff[c];
+    for (int t = threadIdx.x; t < U; t += NT) {
+      const unsigned k = sk[padk<unsigned>(t)];
+      dst[t] = make_int2((int)k, hash_get<unsigned>(S.hk, S.hw, hmask, shift, k));
+    }
+    if (threadIdx.x == 0) ucount[c] = U;
+    __syncthreads();
   }
 }
 
@@ -691,41 +777,34 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   if (rc) return rc;
   const int sms = ctx->num_sms;
   const bool small_ids = n < kSmallIdLimit;
-  const size_t count_smem = small_ids ? sizeof(CountSmem<unsigned>) : sizeof(CountSmem<unsigned long long>);
-  const size_t emit_smem = small_ids ? sizeof(EmitSmem<unsigned>) : sizeof(EmitSmem<unsigned long long>);
-  if (small_ids) {
-    cudaFuncSetAttribute(k_tile_count<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)count_smem);
-    cudaFuncSetAttribute(k_tile_emit<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)emit_smem);
-  } else {
-    cudaFuncSetAttribute(k_tile_count<unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)count_smem);
-    cudaFuncSetAttribute(k_tile_emit<unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)emit_smem);
-  }
-  cudaFuncSetAttribute(k_mid_sort<256, 2 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sizeof(RowSmem<2 * kLongThr>));
-  cudaFuncSetAttribute(k_mid_sort<512, 4 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sizeof(RowSmem<4 * kLongThr>));
-  cudaFuncSetAttribute(k_mid_sort<1024, kChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sizeof(RowSmem<kChunk>));
+  const size_t tile_smem = small_ids ? sizeof(TileSmem<unsigned>) : sizeof(TileSmem<unsigned long long>);
+  if (small_ids)
+    cudaFuncSetAttribute(k_contract_tiles<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem);
+  else
+    cudaFuncSetAttribute(k_contract_tiles<unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tile_smem);
+  cudaFuncSetAttribute(k_mid_rows<256, 2 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(MidSmem<2 * kLongThr>));
+  cudaFuncSetAttribute(k_mid_rows<512, 4 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(MidSmem<4 * kLongThr>));
+  cudaFuncSetAttribute(k_mid_rows<1024, kChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)sizeof(MidSmem<kChunk>));
   cudaFuncSetAttribute(k_long_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem));
 
-  // Pass 1.  Long rows on the auxiliary streams (three size classes; the
-  // chunked rows' sort, merge passes and dedup after the largest class) while
-  // the tiles count the short rows' unique entries on the caller's stream.
-  // Both write ucount; the scan waits for all of them.
+  // Long rows on the auxiliary streams (three size classes; the chunked
+  // rows' sort, merge passes and dedup after the largest class) while the
+  // tiles do the short rows on the caller's stream.  All of them leave their
+  // unique entries in stage1 at eoff[c] (the chunked rows in the stage their
+  // merge parity picks) and their number in ucount[c].
   stage_begin(ctx, s);
   cudaEventRecord(ctx->fork_ev, s);
   for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(ctx->aux[i], ctx->fork_ev, 0);
-  k_mid_sort<256, 2 * kLongThr><<<sms * 4, 256, sizeof(RowSmem<2 * kLongThr>), ctx->aux[0]>>>(
-      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, row_meta, mid_list, mid_ctr + 0, stage1,
-      ucount);
-  k_mid_sort<512, 4 * kLongThr><<<sms * 2, 512, sizeof(RowSmem<4 * kLongThr>), ctx->aux[1]>>>(
-      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, row_meta, mid_list + mid_cap, mid_ctr + 1,
-      stage1, ucount);
-  k_mid_sort<1024, kChunk><<<sms, 1024, sizeof(RowSmem<kChunk>), ctx->aux[2]>>>(
-      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, row_meta, mid_list + 2 * mid_cap,
-      mid_ctr + 2, stage1, ucount);
+  k_mid_rows<256, 2 * kLongThr><<<sms * 4, 256, sizeof(MidSmem<2 * kLongThr>), ctx->aux[0]>>>(
+      fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list, mid_ctr + 0, stage1, ucount);
+  k_mid_rows<512, 4 * kLongThr><<<sms * 2, 512, sizeof(MidSmem<4 * kLongThr>), ctx->aux[1]>>>(
+      fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + mid_cap, mid_ctr + 1, stage1, ucount);
+  k_mid_rows<1024, kChunk><<<sms, 1024, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
+      fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + 2 * mid_cap, mid_ctr + 2, stage1, ucount);
   k_long_sort<<<sms, kChunkThreads, sizeof(ChunkSmem), ctx->aux[2]>>>(
       fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, row_meta, long_list, chunk_row, ctr, stage0);
   ctx->launches += 4;
@@ -750,14 +829,14 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   for (int i = 0; i < 3; ++i) cudaEventRecord(ctx->join_ev[i], ctx->aux[i]);
   // d_sizes[0] holds n' (written by the cmap scan).
   if (small_ids)
-    k_tile_count<unsigned><<<(unsigned)ntiles, kTileThreads, count_smem, s>>>(
-        fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, ucount, st);
+    k_contract_tiles<unsigned><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
+        fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, stage1, ucount, st);
   else
-    k_tile_count<unsigned long long><<<(unsigned)ntiles, kTileThreads, count_smem, s>>>(
-        fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, ucount, st);
+    k_contract_tiles<unsigned long long><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
+        fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, stage1, ucount, st);
   ctx->launches++;
   for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(s, ctx->join_ev[i], 0);
-  stage_end(ctx, CM_STAGE_TILE_COUNT, s);
+  stage_end(ctx, CM_STAGE_TILES, s);
 
   // cxadj = exclusive scan of ucount; d_sizes[1] = m'.
   stage_begin(ctx, s);
@@ -766,25 +845,18 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   ctx->launches++;
   stage_end(ctx, CM_STAGE_SCAN, s);
 
-  // Pass 2.  Tiles sort, merge and write the short rows; the long rows'
-  // unique entries are copied out on an auxiliary stream meanwhile.
+  // Every row's unique entries to their final place.
   stage_begin(ctx, s);
   cudaEventRecord(ctx->fork_ev, s);
   cudaStreamWaitEvent(ctx->aux[0], ctx->fork_ev, 0);
   k_long_copy<<<sms * 4, 256, 0, ctx->aux[0]>>>(long_list, chunk_row, eoff, ctr, mid_list, mid_ctr, (int)mid_cap,
                                                  stage0, stage1, ucount, coarse->xadj, coarse->adjncy, coarse->adjwgt);
   cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
-  if (small_ids)
-    k_tile_emit<unsigned><<<(unsigned)ntiles, kTileThreads, emit_smem, s>>>(
-        fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, coarse->xadj, coarse->adjncy,
-        coarse->adjwgt, st);
-  else
-    k_tile_emit<unsigned long long><<<(unsigned)ntiles, kTileThreads, emit_smem, s>>>(
-        fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, coarse->xadj, coarse->adjncy,
-        coarse->adjwgt, st);
+  k_copy_tiles<<<(unsigned)ntiles, kTileThreads, 0, s>>>(eoff, d_sizes, first_row, ucount, coarse->xadj, stage1,
+                                                         coarse->adjncy, coarse->adjwgt);
   ctx->launches += 2;
   cudaStreamWaitEvent(s, ctx->join_ev[0], 0);
-  stage_end(ctx, CM_STAGE_TILE_EMIT, s);
+  stage_end(ctx, CM_STAGE_COPY, s);
   return check_launch(ctx, "contract");
 }
 

@@ -258,7 +258,7 @@ extern "C" int cm_ctx_match_trace(cm_ctx *ctx, int64_t *out, int32_t cap_rows, i
 }
 
 extern "C" const char *cm_stage_name(int32_t stage) {
-  static const char *names[CM_STAGE_COUNT] = {"k_match", "k_cmap", "k_tile_count", "k_count_scan", "k_tile_emit"};
+  static const char *names[CM_STAGE_COUNT] = {"k_match", "k_cmap", "k_contract_tiles", "k_count_scan", "k_copy_tiles"};
   return stage >= 0 && stage < CM_STAGE_COUNT ? names[stage] : "";
 }
 
