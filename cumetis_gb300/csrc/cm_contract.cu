@@ -43,7 +43,6 @@ constexpr int kTileCap = kTileDiag + kLongThr;    // max entries in a tile (mult
 constexpr int kHashCap = 4096;                    // count-pass hash slots (power of two >= 2 kTileCap)
 constexpr int kChunk = 8192;                      // long-row chunk (entries sorted per block)
 constexpr int kChunkThreads = 1024;
-constexpr unsigned kSelfKey = 0xffffffffu;        // self loops sort last in their row
 
 // Composite key (tile-local row, coarse id).  32-bit when coarse ids fit in
 // 23 bits (n < 2^23 - 1; rows need 9 bits for kTileDiag = 512), else 64-bit.
@@ -403,12 +402,6 @@ k_copy_tiles(const int *__restrict__ eoff, const int *d_cn, const int *__restric
 // ---------------------------------------------------------------------------
 // Long rows
 // ---------------------------------------------------------------------------
-template <int CAP>
-struct RowSmem {
-  unsigned long long v[2][padded_size(CAP + 8)];  // packed (coarse id << 32 | weight) at pad16(i); +8 for hs[cnt]
-};
-using ChunkSmem = RowSmem<kChunk>;
-
 // Passes a row of length L needs before its chunks form one sorted run.
 __host__ __device__ __forceinline__ int merge_passes(int L) {
   int p = 0;
@@ -417,74 +410,20 @@ __host__ __device__ __forceinline__ int merge_passes(int L) {
   return p;
 }
 
-// Gathers entries [cs, cs+cnt) of coarse row c's expanded row into shared
-// memory and sorts them.  If `whole` (the segment is the entire row), merges
-// duplicates and writes the unique entries to dedup_dst and their count to
-// *ucount_c; otherwise writes the sorted run to run_dst.
-template <int NT, int CAP>
-__device__ __forceinline__ void sort_row_segment(RowSmem<CAP> &S, int *scan, int c, int xl, int dl, int xf, int cs,
-                                                 int cnt, bool whole, int2 *run_dst, int2 *dedup_dst, int *ucount_c,
-                                                 const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
-                                                 const int *__restrict__ cmap) {
-  for (int t0 = threadIdx.x; t0 < cnt; t0 += 4 * NT) {
-    int src[4], x[4], w[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int t = t0 + u * NT;
-      src[u] = t < cnt ? expanded_src(cs + t, xl, dl, xf) : -1;
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      x[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
-      w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : 0;
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int t = t0 + u * NT;
-      if (t < cnt) {
-        const unsigned key = x[u] == c ? kSelfKey : (unsigned)x[u];
-        S.v[0][pad16(t)] = ((unsigned long long)key << 32) | (unsigned)w[u];
-      }
-    }
-  }
-  __syncthreads();
-  const int b = block_merge_sort_packed<NT, 8>(S.v[0], S.v[1], cnt);
-  const unsigned long long *P = S.v[b];
-  if (!whole) {
-    for (int t = threadIdx.x; t < cnt; t += NT) {
-      const unsigned long long e = P[pad16(t)];
-      run_dst[t] = make_int2((int)(unsigned)(e >> 32), (int)(unsigned)e);
-    }
-  } else {
-    int *hs = reinterpret_cast<int *>(S.v[b ^ 1]);
-    const int ipt = (cnt + NT - 1) / NT;
-    const int i0 = min(cnt, (int)threadIdx.x * ipt), i1 = min(cnt, i0 + ipt);
-    auto head = [&](int i) {
-      const unsigned k = (unsigned)(P[pad16(i)] >> 32);
-      return k != kSelfKey && (i == 0 || (unsigned)(P[pad16(i - 1)] >> 32) != k);
-    };
-    int hc = 0;
-    for (int i = i0; i < i1; ++i) hc += head(i);
-    int tot;
-    int run = block_exclusive_scan<NT>(hc, scan, &tot);
-    for (int i = i0; i < i1; ++i) {
-      hs[i] = run;
-      run += head(i);
-    }
-    if (threadIdx.x == 0) { hs[cnt] = tot; *ucount_c = tot; }
-    __syncthreads();
-    for (int i = threadIdx.x; i < cnt; i += NT) {
-      if (hs[i + 1] == hs[i]) continue;
-      const unsigned k = (unsigned)(P[pad16(i)] >> 32);
-      unsigned sum = (unsigned)P[pad16(i)];
-      for (int j = i + 1; j < cnt && (unsigned)(P[pad16(j)] >> 32) == k; ++j) sum += (unsigned)P[pad16(j)];
-      dedup_dst[hs[i]] = make_int2((int)k, (int)sum);
-    }
-  }
-  __syncthreads();
+// Chunked rows carry packed entries (coarse id << 32 | weight) through the
+// sort and merge passes.  A self loop gets the id kSelfKey: it sorts after
+// every coarse id (< 2^31) and keeps the packed word below the all-ones pad.
+constexpr unsigned kSelfKey = 0xfffffffeu;
+__device__ __forceinline__ unsigned long long pack_entry(int2 e) {
+  return ((unsigned long long)(unsigned)e.x << 32) | (unsigned)e.y;
 }
+__device__ __forceinline__ int2 unpack_entry(unsigned long long v) {
+  return make_int2((int)(unsigned)(v >> 32), (int)(unsigned)v);
+}
+
+struct ChunkSmem {
+  unsigned long long v[2][padded_k<unsigned long long>(kChunk)];
+};
 
 // Rows too long for a tile but <= kChunk entries, one size class per launch:
 // one block merges one whole row's duplicates in a shared-memory hash set,
@@ -554,18 +493,17 @@ k_mid_rows(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const
   }
 }
 
-// Rows longer than kChunk: each kChunk-entry chunk sorted into stage0 as one
-// run for the merge passes.
+// Rows longer than kChunk: each chunk of kChunk entries is gathered, sorted
+// in shared memory (warp-register runs, then merge passes) and written to
+// stage0 as one run for the merge passes.
 __global__ void __launch_bounds__(kChunkThreads, 1)
-k_long_sort(const int *__restrict__ xadj, const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
-            const int *__restrict__ match, const int *__restrict__ cmap, const int *__restrict__ leader,
+k_long_sort(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
             const int *__restrict__ eoff, const int4 *__restrict__ row_meta, const int *__restrict__ long_list,
-            const int *__restrict__ chunk_row, const unsigned long long *long_ctr, int2 *__restrict__ stage) {
+            const int *__restrict__ chunk_row, const unsigned long long *long_ctr, int2 *__restrict__ stage,
+            int *__restrict__ ucount) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem &S = *reinterpret_cast<ChunkSmem *>(smem_raw);
-  __shared__ int scan[kChunkThreads / 32 + 1];
-  const unsigned long long ctr = *long_ctr;
-  const int nchunks = (int)(ctr & 0xffffffffu);
+  const int nchunks = (int)(*long_ctr & 0xffffffffu);
   for (int q = blockIdx.x; q < nchunks; q += gridDim.x) {
     const int idx = chunk_row[q];
     const int c = long_list[2 * idx];
@@ -573,33 +511,68 @@ k_long_sort(const int *__restrict__ xadj, const int *__restrict__ adjncy, const 
     const int j = q - long_list[2 * idx + 1];
     const int cs = j * kChunk;
     const int cnt = min(kChunk, md.w - cs);
-    sort_row_segment<kChunkThreads, kChunk>(S, scan, c, md.x, md.y, md.z, cs, cnt, false, stage + eoff[c] + cs,
-                                            nullptr, nullptr, adjncy, adjwgt, cmap);
+    if (j == 0 && threadIdx.x == 0) ucount[c] = 0;  // the dedup adds the chunks' counts
+    for (int t0 = threadIdx.x; t0 < cnt; t0 += 4 * kChunkThreads) {
+      int src[4], x[4], w[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int t = t0 + u * kChunkThreads;
+        src[u] = t < cnt ? expanded_src(cs + t, md.x, md.y, md.z) : -1;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        x[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
+        w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int t = t0 + u * kChunkThreads;
+        if (t < cnt) S.v[0][padk<unsigned long long>(t)] = pack_entry(make_int2(x[u] == c ? (int)kSelfKey : x[u], w[u]));
+      }
+    }
+    __syncthreads();
+    const int b = block_sort_keys<unsigned long long, kChunkThreads, 8>(S.v[0], S.v[1], cnt);
+    int2 *dst = stage + eoff[c] + cs;
+    for (int t = threadIdx.x; t < cnt; t += kChunkThreads) dst[t] = unpack_entry(S.v[b][padk<unsigned long long>(t)]);
+    __syncthreads();
   }
 }
 
+// Items of merge(A[0..alen), B[0..blen)) taken from A among the first diag
+// outputs (A wins ties), on packed entries in global memory.
 __device__ __forceinline__ int merge_path_g(const int2 *A, int alen, const int2 *B, int blen, int diag) {
   int lo = diag > blen ? diag - blen : 0;
   int hi = diag < alen ? diag : alen;
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
-    if ((unsigned)__ldcg(&A[mid].x) <= (unsigned)__ldcg(&B[diag - 1 - mid].x)) lo = mid + 1;
+    if (pack_entry(__ldcg(&A[mid])) <= pack_entry(__ldcg(&B[diag - 1 - mid]))) lo = mid + 1;
     else hi = mid;
   }
   return lo;
 }
 
 // All long rows' merge passes in one cooperative launch: pass p merges run
-// pairs of width kChunk << p; blocks take kChunk-sized output blocks, threads
-// 16 outputs each (merge path per thread).  Rows already a single run skip.
+// pairs of width kChunk << p.  A block produces one kChunk-sized block of
+// output: two threads find where it starts and ends in the two runs (merge
+// path over global memory), the block loads both windows into shared memory,
+// every thread merges kMergePer outputs there, and the block stores the
+// result coalesced.  Rows already a single run skip.
 constexpr int kMergeThreads = 512;
 constexpr int kMergePer = kChunk / kMergeThreads;  // 16
+struct MergeSmem {
+  unsigned long long win[padded_k<unsigned long long>(kChunk)];
+  unsigned long long out[padded_k<unsigned long long>(kChunk)];
+  int cut[4];
+};
 
 __global__ void __launch_bounds__(kMergeThreads)
 k_long_merge(const int *__restrict__ long_list, const int *__restrict__ chunk_row, const int *__restrict__ eoff,
              const unsigned long long *long_ctr, int2 *stage0, int2 *stage1, DevStatus *st) {
-  const unsigned long long ctr = *long_ctr;
-  const int nchunks = (int)(ctr & 0xffffffffu);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  MergeSmem &S = *reinterpret_cast<MergeSmem *>(smem_raw);
+  const int nchunks = (int)(*long_ctr & 0xffffffffu);
   const int npass = merge_passes(st->max_row);
   for (int p = 0; p < npass; ++p) {
     const long long width = (long long)kChunk << p;
@@ -609,63 +582,88 @@ k_long_merge(const int *__restrict__ long_list, const int *__restrict__ chunk_ro
       const int idx = chunk_row[q];
       const int c = long_list[2 * idx];
       const int L = eoff[c + 1] - eoff[c];
-      if (L <= width) continue;
-      // Rows that finished earlier have their data in the other stage; a
-      // row is merged in pass p only while it still has more than one run.
+      // A row is merged in pass p only while it still has more than one run;
+      // rows that finished earlier keep their data in the stage of their parity.
       if (merge_passes(L) <= p) continue;
       const int j = q - long_list[2 * idx + 1];
       const long long base = eoff[c];
-      const int out0 = j * kChunk + threadIdx.x * kMergePer;
-      if (out0 >= L) continue;
-      const int ps = (int)((out0 / (2 * width)) * (2 * width));
+      const int o0 = j * kChunk;
+      const int ps = (int)((o0 / (2 * width)) * (2 * width));
       const int alen = (int)min(width, (long long)(L - ps));
       const int blen = (int)min(width, (long long)(L - ps - alen));
       const int2 *A = src + base + ps;
       const int2 *B = A + alen;
-      const int diag = out0 - ps;
-      int i = blen == 0 ? diag : merge_path_g(A, alen, B, blen, diag);
-      int jj = diag - i;
-      const int nout = min(kMergePer, L - out0);
-      int2 a = i < alen ? __ldcg(A + i) : make_int2(0, 0);
-      int2 bb = jj < blen ? __ldcg(B + jj) : make_int2(0, 0);
-      for (int t = 0; t < nout; ++t) {
-        const bool takeA = (jj >= blen) || (i < alen && (unsigned)a.x <= (unsigned)bb.x);
-        if (takeA) {
-          dst[base + out0 + t] = a;
-          ++i;
-          if (i < alen) a = __ldcg(A + i);
-        } else {
-          dst[base + out0 + t] = bb;
-          ++jj;
-          if (jj < blen) bb = __ldcg(B + jj);
+      const int d0 = o0 - ps, d1 = min(o0 + kChunk, ps + alen + blen) - ps;
+      const int nout = d1 - d0;
+      if (threadIdx.x < 2) {
+        const int d = threadIdx.x == 0 ? d0 : d1;
+        S.cut[threadIdx.x] = blen == 0 ? min(d, alen) : merge_path_g(A, alen, B, blen, d);
+      }
+      __syncthreads();
+      const int i0 = S.cut[0], i1 = S.cut[1];
+      const int na = i1 - i0, nb = nout - na;
+      const int j0 = d0 - i0;
+      for (int t = threadIdx.x; t < na; t += kMergeThreads) S.win[padk<unsigned long long>(t)] = pack_entry(__ldcg(A + i0 + t));
+      for (int t = threadIdx.x; t < nb; t += kMergeThreads)
+        S.win[padk<unsigned long long>(na + t)] = pack_entry(__ldcg(B + j0 + t));
+      __syncthreads();
+      const int od = threadIdx.x * kMergePer;
+      if (od < nout) {
+        int lo = od > nb ? od - nb : 0, hi = od < na ? od : na;
+        while (lo < hi) {
+          const int mid = (lo + hi) >> 1;
+          if (S.win[padk<unsigned long long>(mid)] <= S.win[padk<unsigned long long>(na + od - 1 - mid)]) lo = mid + 1;
+          else hi = mid;
+        }
+        int ia = lo, ib = od - lo;
+        const unsigned long long kMax = ~0ull;
+        unsigned long long ka = ia < na ? S.win[padk<unsigned long long>(ia)] : kMax;
+        unsigned long long kb = ib < nb ? S.win[padk<unsigned long long>(na + ib)] : kMax;
+        const int cnt = min(kMergePer, nout - od);
+        for (int t = 0; t < cnt; ++t) {
+          const bool takeA = (ib >= nb) || (ia < na && ka <= kb);
+          S.out[padk<unsigned long long>(od + t)] = takeA ? ka : kb;
+          if (takeA) { ++ia; ka = ia < na ? S.win[padk<unsigned long long>(ia)] : kMax; }
+          else { ++ib; kb = ib < nb ? S.win[padk<unsigned long long>(na + ib)] : kMax; }
         }
       }
+      __syncthreads();
+      int2 *o = dst + base + ps + d0;
+      for (int t = threadIdx.x; t < nout; t += kMergeThreads) o[t] = unpack_entry(S.out[padk<unsigned long long>(t)]);
+      __syncthreads();
     }
     if (p + 1 < npass && !grid_barrier(st, gridDim.x)) return;
   }
 }
 
-// Deduplicates each long row (sorted, in stage[merge_passes(L) & 1]) into the
-// other stage, compacted at eoff[c]; ucount[c] = unique entries.
+// Merges duplicates of the chunked rows, one block per chunk of the sorted row
+// (in stage[merge_passes(L) & 1]): a head is the first entry of a run of equal
+// ids that is not a self loop; each head's run (which may reach into the next
+// chunk) is summed and written, compacted within the chunk, to the other stage
+// at eoff[c] + j*kChunk.  chunk_cnt[q] = the chunk's unique entries, also added
+// to ucount[c].
 constexpr int kDedupThreads = 512;
 __global__ void __launch_bounds__(kDedupThreads)
-k_long_dedup(const int *__restrict__ long_list, const int *__restrict__ eoff, const unsigned long long *long_ctr,
-             int2 *stage0, int2 *stage1, int *__restrict__ ucount) {
+k_long_dedup(const int *__restrict__ long_list, const int *__restrict__ chunk_row, const int *__restrict__ eoff,
+             const unsigned long long *long_ctr, const int2 *stage0, const int2 *stage1, int2 *out0, int2 *out1,
+             int *__restrict__ chunk_cnt, int *__restrict__ ucount) {
   __shared__ int scan[kDedupThreads / 32 + 1];
-  const int nlong = (int)(*long_ctr >> 32);
-  for (int idx = blockIdx.x; idx < nlong; idx += gridDim.x) {
+  const int nchunks = (int)(*long_ctr & 0xffffffffu);
+  for (int q = blockIdx.x; q < nchunks; q += gridDim.x) {
+    const int idx = chunk_row[q];
     const int c = long_list[2 * idx];
     const int L = eoff[c + 1] - eoff[c];
-    if (L <= kChunk) continue;  // (not in this list)
+    const int j = q - long_list[2 * idx + 1];
     const int fb = merge_passes(L) & 1;
     const int2 *src = (fb ? stage1 : stage0) + eoff[c];
-    int2 *dst = (fb ? stage0 : stage1) + eoff[c];
+    int2 *dst = (fb ? out0 : out1) + eoff[c] + (long long)j * kChunk;
+    const int lo = j * kChunk, hi = min(L, lo + kChunk);
     int carry = 0;
-    for (int b = 0; b < L; b += kDedupThreads) {
+    for (int b = lo; b < hi; b += kDedupThreads) {
       const int i = b + threadIdx.x;
       int h = 0;
       int2 e = make_int2(0, 0);
-      if (i < L) {
+      if (i < hi) {
         e = src[i];
         h = ((unsigned)e.x != kSelfKey) && (i == 0 || src[i - 1].x != e.x);
       }
@@ -673,47 +671,62 @@ k_long_dedup(const int *__restrict__ long_list, const int *__restrict__ eoff, co
       const int ex = block_exclusive_scan<kDedupThreads>(h, scan, &tot);
       if (h) {
         unsigned sum = (unsigned)e.y;
-        for (int j = i + 1; j < L && src[j].x == e.x; ++j) sum += (unsigned)src[j].y;
+        for (int k = i + 1; k < L && src[k].x == e.x; ++k) sum += (unsigned)src[k].y;
         dst[carry + ex] = make_int2(e.x, (int)sum);
       }
       carry += tot;
     }
-    if (threadIdx.x == 0) ucount[c] = carry;
+    if (threadIdx.x == 0) {
+      chunk_cnt[q] = carry;
+      atomicAdd(&ucount[c], carry);
+    }
   }
 }
 
-// Copies every long row's unique entries to its final place once the tiles
-// have fixed cxadj: first the size-class rows (stage1), then the chunked rows.
+// Copies every long row's unique entries to its final place once cxadj is
+// known: first the size-class rows (stage1 at eoff[c]), then the chunks of the
+// chunked rows (each at cxadj[c] + the unique entries of the row's earlier
+// chunks).
 __global__ void k_long_copy(const int *__restrict__ long_list, const int *__restrict__ chunk_row,
                             const int *__restrict__ eoff, const unsigned long long *long_ctr,
                             const int *__restrict__ mid_list, const int *__restrict__ mid_ctr, int mid_cap,
-                            const int2 *stage0, const int2 *stage1, const int *__restrict__ ucount,
-                            const int *__restrict__ cxadj, int *__restrict__ cadjncy, int *__restrict__ cadjwgt) {
+                            const int2 *stage0, const int2 *stage1, const int *__restrict__ chunk_cnt,
+                            const int *__restrict__ ucount, const int *__restrict__ cxadj, int *__restrict__ cadjncy,
+                            int *__restrict__ cadjwgt) {
+  __shared__ int s_pre[32];
   const int n0 = mid_ctr[0], n1 = mid_ctr[1], n2 = mid_ctr[2];
   const int nmid = n0 + n1 + n2;
   const int nchunks = (int)(*long_ctr & 0xffffffffu);
   for (int q = blockIdx.x; q < nmid + nchunks; q += gridDim.x) {
-    int c, lo, hi;
+    int cnt;
+    long long dst;
     const int2 *src;
     if (q < nmid) {
       const int cls = q < n0 ? 0 : (q < n0 + n1 ? 1 : 2);
       const int i = q - (cls == 0 ? 0 : (cls == 1 ? n0 : n0 + n1));
-      c = mid_list[(size_t)cls * mid_cap + i];
+      const int c = mid_list[(size_t)cls * mid_cap + i];
       src = stage1 + eoff[c];
-      lo = 0;
-      hi = ucount[c];
+      cnt = ucount[c];
+      dst = cxadj[c];
     } else {
       const int qq = q - nmid;
       const int idx = chunk_row[qq];
-      c = long_list[2 * idx];
+      const int c = long_list[2 * idx];
+      const int first = long_list[2 * idx + 1];
       const int L = eoff[c + 1] - eoff[c];
-      src = ((merge_passes(L) & 1) ? stage0 : stage1) + eoff[c];
-      const int j = qq - long_list[2 * idx + 1];
-      lo = j * kChunk;
-      hi = min(ucount[c], (j + 1) * kChunk);
+      src = ((merge_passes(L) & 1) ? stage0 : stage1) + eoff[c] + (long long)(qq - first) * kChunk;
+      cnt = chunk_cnt[qq];
+      int pre = 0;
+      for (int k = first + threadIdx.x; k < qq; k += blockDim.x) pre += chunk_cnt[k];
+      pre = __reduce_add_sync(0xffffffffu, pre);
+      if ((threadIdx.x & 31) == 0) s_pre[threadIdx.x >> 5] = pre;
+      __syncthreads();
+      pre = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) pre += s_pre[w];
+      __syncthreads();
+      dst = (long long)cxadj[c] + pre;
     }
-    const long long dst = cxadj[c];
-    for (int t = lo + threadIdx.x; t < hi; t += blockDim.x) {
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
       const int2 e = src[t];
       cadjncy[dst + t] = e.x;
       cadjwgt[dst + t] = e.y;
@@ -731,7 +744,7 @@ size_t contract_ws_bytes(int64_t n, int64_t m) {
   b += (size_t)(ntiles + 2) * 4 + 256;       // first_row
   b += (size_t)(m / kChunk + 2) * 8 + 256;   // long_list
   b += (size_t)(m / (kLongThr + 1) + 2) * 12 + 256;  // size-class lists
-  b += (size_t)nchunks * 4 + 256;            // chunk_row
+  b += (size_t)nchunks * 4 * 2 + 512;        // chunk_row, chunk_cnt
   b += 256;                                  // counters
   b += (size_t)(ntiles + 2) * 8 + 256;       // tile look-back
   b += (size_t)n * 16 + 256;                 // row metadata
@@ -757,13 +770,14 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   int *first_row = (int *)ws_take(ctx, (size_t)(ntiles + 2) * 4);
   int *long_list = (int *)ws_take(ctx, (size_t)(m / kChunk + 2) * 8);
   int *chunk_row = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
+  int *chunk_cnt = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
   int *mid_list = (int *)ws_take(ctx, (size_t)mid_cap * 3 * 4);
   int4 *row_meta = (int4 *)ws_take(ctx, (size_t)n * 16);
   unsigned long long *ctr = (unsigned long long *)ws_take(ctx, 64);   // [0] chunked rows, [1] mid counters
   unsigned long long *lb = (unsigned long long *)ws_take(ctx, (size_t)(ntiles + 2) * 8);
   int2 *stage0 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
   int2 *stage1 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
-  if (!leader || !ucount || !eoff || !first_row || !long_list || !chunk_row || !mid_list || !row_meta || !ctr || !lb ||
+  if (!leader || !ucount || !eoff || !first_row || !long_list || !chunk_row || !chunk_cnt || !mid_list || !row_meta || !ctr || !lb ||
       !stage0 || !stage1)
     return cm_fail(CM_ERR_NOMEM, "contract: workspace too small");
   int *mid_ctr = reinterpret_cast<int *>(ctr + 1);
@@ -790,6 +804,7 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   cudaFuncSetAttribute(k_mid_rows<1024, kChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(MidSmem<kChunk>));
   cudaFuncSetAttribute(k_long_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem));
+  cudaFuncSetAttribute(k_long_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MergeSmem));
 
   // Long rows on the auxiliary streams (three size classes; the chunked
   // rows' sort, merge passes and dedup after the largest class) while the
@@ -806,11 +821,11 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   k_mid_rows<1024, kChunk><<<sms, 1024, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
       fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + 2 * mid_cap, mid_ctr + 2, stage1, ucount);
   k_long_sort<<<sms, kChunkThreads, sizeof(ChunkSmem), ctx->aux[2]>>>(
-      fine->xadj, fine->adjncy, fine->adjwgt, match, cmap, leader, eoff, row_meta, long_list, chunk_row, ctr, stage0);
+      fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, long_list, chunk_row, ctr, stage0, ucount);
   ctx->launches += 4;
   {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_long_merge, kMergeThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_long_merge, kMergeThreads, sizeof(MergeSmem));
     int grid = sms * (per_sm > 0 ? per_sm : 1);
     const int *a0 = long_list;
     const int *a1 = chunk_row;
@@ -819,12 +834,13 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
     int2 *a4 = stage0, *a5 = stage1;
     DevStatus *a6 = st;
     void *args[] = {(void *)&a0, (void *)&a1, (void *)&a2, (void *)&a3, (void *)&a4, (void *)&a5, (void *)&a6};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_long_merge, dim3(grid), dim3(kMergeThreads), args, 0,
-                                                ctx->aux[2]);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_long_merge, dim3(grid), dim3(kMergeThreads), args,
+                                                sizeof(MergeSmem), ctx->aux[2]);
     if (e != cudaSuccess) return cuda_status(e, "contract: long-row merge launch");
     ctx->launches++;
   }
-  k_long_dedup<<<sms * 2, kDedupThreads, 0, ctx->aux[2]>>>(long_list, eoff, ctr, stage0, stage1, ucount);
+  k_long_dedup<<<sms * 4, kDedupThreads, 0, ctx->aux[2]>>>(long_list, chunk_row, eoff, ctr, stage0, stage1, stage0,
+                                                            stage1, chunk_cnt, ucount);
   ctx->launches++;
   for (int i = 0; i < 3; ++i) cudaEventRecord(ctx->join_ev[i], ctx->aux[i]);
   // d_sizes[0] holds n' (written by the cmap scan).
@@ -850,7 +866,8 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   cudaEventRecord(ctx->fork_ev, s);
   cudaStreamWaitEvent(ctx->aux[0], ctx->fork_ev, 0);
   k_long_copy<<<sms * 4, 256, 0, ctx->aux[0]>>>(long_list, chunk_row, eoff, ctr, mid_list, mid_ctr, (int)mid_cap,
-                                                 stage0, stage1, ucount, coarse->xadj, coarse->adjncy, coarse->adjwgt);
+                                                 stage0, stage1, chunk_cnt, ucount, coarse->xadj, coarse->adjncy,
+                                                 coarse->adjwgt);
   cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
   k_copy_tiles<<<(unsigned)ntiles, kTileThreads, 0, s>>>(eoff, d_sizes, first_row, ucount, coarse->xadj, stage1,
                                                          coarse->adjncy, coarse->adjwgt);
