@@ -494,7 +494,7 @@ k_mid_rows(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const
 }
 
 // Rows longer than kChunk: each chunk of kChunk entries is gathered, sorted
-// in shared memory (warp-register runs, then merge passes) and written to
+// in shared memory (register runs of 8, then merge passes) and written to
 // stage0 as one run for the merge passes.
 __global__ void __launch_bounds__(kChunkThreads, 1)
 k_long_sort(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
@@ -533,7 +533,7 @@ k_long_sort(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, cons
       }
     }
     __syncthreads();
-    const int b = block_sort_keys<unsigned long long, kChunkThreads, 8>(S.v[0], S.v[1], cnt);
+    const int b = block_merge_sort_packed<kChunkThreads, 8>(S.v[0], S.v[1], cnt);
     int2 *dst = stage + eoff[c] + cs;
     for (int t = threadIdx.x; t < cnt; t += kChunkThreads) dst[t] = unpack_entry(S.v[b][padk<unsigned long long>(t)]);
     __syncthreads();
