@@ -37,6 +37,20 @@ class cm_coarsen_params(ctypes.Structure):
                 ("max_levels", ctypes.c_int32), ("shrink", ctypes.c_double)]
 
 
+class cm_part_params(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_int32), ("match_mode", ctypes.c_int32), ("refine_passes", ctypes.c_int32),
+                ("coarsen_to", ctypes.c_int32)]
+
+
+class cm_part_stats(ctypes.Structure):
+    _fields_ = [("coarsen_ms", ctypes.c_double), ("init_ms", ctypes.c_double), ("uncoarsen_ms", ctypes.c_double),
+                ("total_ms", ctypes.c_double), ("levels", ctypes.c_int32), ("coarsest_nvtxs", ctypes.c_int32),
+                ("initial_cut", ctypes.c_int32), ("edge_cut", ctypes.c_int64), ("moves", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 _lib = None
 
 
@@ -72,6 +86,7 @@ def _declare(L):
         "cm_write_partition": (c_int, [ctypes.c_char_p, c_i32, c_i32, _I32P]),
         "cm_edge_cut": (c_i64, [G, _I32P]),
         "cm_imbalance": (ctypes.c_double, [G, c_i32, _I32P]),
+        "cm_initial_partition": (c_int, [G, c_i32, ctypes.c_uint32, _I32P, _I32P]),
     }
     optional = {
         "cm_ctx_create": (c_int, [c_int, ctypes.POINTER(c_vp)]),
@@ -94,6 +109,12 @@ def _declare(L):
         "cm_ctx_set_match_trace": (c_int, [c_vp, c_i32]),
         "cm_ctx_match_trace": (c_int, [c_vp, ctypes.POINTER(ctypes.c_int64), c_i32, _I32P]),
         "cm_hierarchy_read_level": (c_int, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp]),
+        "cm_refine_kway": (c_int, [c_vp, G, c_i32, c_vp, ctypes.POINTER(c_i64), c_vp]),
+        "cm_project": (c_int, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp]),
+        "cm_part_default_params": (None, [ctypes.POINTER(cm_part_params)]),
+        "cm_part_graph": (c_int, [c_vp, c_i32, _I32P, _I32P, _I32P, _I32P, c_i32, c_vp, c_vp, _I32P, _I32P,
+                                  ctypes.POINTER(cm_part_params), ctypes.POINTER(cm_part_stats)]),
+        "cuMetis_PartGraph": (c_int, [_I32P, _I32P, _I32P, _I32P, _I32P, _I32P, c_vp, c_vp, _I32P, _I32P]),
     }
     for name, (res, args) in list(sigs.items()) + list(optional.items()):
         fn = getattr(L, name, None)
@@ -227,6 +248,17 @@ def read_graph(path):
 def write_partition(graph_path, nparts, part):
     part = _i32(part)
     _check(lib().cm_write_partition(graph_path.encode(), int(nparts), len(part), _np_p(part)))
+
+
+def initial_partition(g, nparts, seed=1):
+    """Initial partition of a host Graph by recursive bisection (host code,
+    the reference's cuMetis_rbbisection restated).  Returns (part, objval)."""
+    part = np.zeros(max(g.nvtxs, 1), np.int32)
+    obj = np.zeros(1, np.int32)
+    cg = g.as_cm()
+    _check(lib().cm_initial_partition(ctypes.byref(cg), int(nparts), ctypes.c_uint32(seed), _np_p(part),
+                                      _np_p(obj)))
+    return part[:g.nvtxs], int(obj[0])
 
 
 def coarsen_threshold(nvtxs, nparts):

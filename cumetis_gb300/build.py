@@ -19,8 +19,8 @@ LIB = os.path.join(HERE, "libcm.so")
 CLI = os.path.join(HERE, "cuMetis")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["cm_ctx.cu", "cm_match.cu", "cm_cmap.cu", "cm_contract.cu"]
-CPP_SOURCES = ["cm_graph.cpp"]
+CU_SOURCES = ["cm_ctx.cu", "cm_match.cu", "cm_cmap.cu", "cm_contract.cu", "cm_refine.cu"]
+CPP_SOURCES = ["cm_graph.cpp", "cm_initpart.cpp"]
 CLI_SOURCES = ["cm_cli.cpp"]
 
 

@@ -89,19 +89,7 @@ void stage_end(cm_ctx *ctx, int stage, cudaStream_t s) {
   if (ctx->pending.size() > 4096) drain_pending(ctx);
 }
 
-namespace {
-
-size_t level_ws_bytes(int64_t n, int64_t m) {
-  // matching and contraction run one after the other and share the workspace
-  return std::max(match_ws_bytes(n, m), contract_ws_bytes(n, m) + 1024);
-}
-
 int set_device(cm_ctx *ctx) { return cuda_status(cudaSetDevice(ctx->device), "cudaSetDevice"); }
-
-bool bad_graph(const cm_graph *g) {
-  return !g || g->nvtxs < 0 || g->nedges < 0 ||
-         (g->nvtxs > 0 && (!g->xadj || !g->vwgt)) || (g->nedges > 0 && (!g->adjncy || !g->adjwgt));
-}
 
 // Reads the device status, clears its error, returns it as a CM status.
 int take_device_error(cm_ctx *ctx, cudaStream_t s) {
@@ -121,6 +109,18 @@ int take_device_error(cm_ctx *ctx, cudaStream_t s) {
     return cm_fail(err, "device reported error %d at %s", err, (site >= 0 && site <= 5) ? sites[site] : "?");
   }
   return CM_OK;
+}
+
+namespace {
+
+size_t level_ws_bytes(int64_t n, int64_t m) {
+  // matching and contraction run one after the other and share the workspace
+  return std::max(match_ws_bytes(n, m), contract_ws_bytes(n, m) + 1024);
+}
+
+bool bad_graph(const cm_graph *g) {
+  return !g || g->nvtxs < 0 || g->nedges < 0 ||
+         (g->nvtxs > 0 && (!g->xadj || !g->vwgt)) || (g->nedges > 0 && (!g->adjncy || !g->adjwgt));
 }
 
 __global__ void k_sum_i32(const int *a, long long n, unsigned long long *out) {

@@ -49,6 +49,12 @@ inline void ws_reset(cm_ctx *ctx) { ctx->ws_used = 0; }
 void stage_begin(cm_ctx *ctx, cudaStream_t s);
 void stage_end(cm_ctx *ctx, int stage, cudaStream_t s);
 
+// Makes the context's device current.
+int set_device(cm_ctx *ctx);
+// Reads the device status block on stream s, clears a recorded error and
+// returns it as a CM status (CM_OK when none).
+int take_device_error(cm_ctx *ctx, cudaStream_t s);
+
 // Records the CUDA error (if any) as the thread's last error; returns a status.
 int cuda_status(cudaError_t e, const char *what);
 int check_launch(cm_ctx *ctx, const char *what);

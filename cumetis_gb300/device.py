@@ -132,6 +132,33 @@ class Context:
         return DeviceGraph(cx[:cn + 1], ca[:cm_], cw[:cm_], cv[:cn]), cmap[:n]
 
     # ---- multilevel -------------------------------------------------------
+    def part_graph(self, g, nparts, seed=1, mode=MATCH_HEM, refine_passes=1, coarsen_to=0):
+        """k-way partition of a host Graph (cm_part_graph).  Returns
+        (part, edge_cut, stats dict)."""
+        from . import cm_part_params, cm_part_stats, _np_p
+        p = cm_part_params(int(seed), int(mode), int(refine_passes), int(coarsen_to))
+        st = cm_part_stats()
+        part = np.zeros(max(g.nvtxs, 1), np.int32)
+        obj = np.zeros(1, np.int32)
+        _check(lib().cm_part_graph(self._h, g.nvtxs, _np_p(g.xadj), _np_p(g.adjncy), _np_p(g.vwgt),
+                                   _np_p(g.adjwgt), int(nparts), None, None, _np_p(obj), _np_p(part),
+                                   ctypes.byref(p), ctypes.byref(st)))
+        return part[:g.nvtxs], int(obj[0]), st.as_dict()
+
+    def refine_kway(self, g_dev, nparts, d_where, stream=None):
+        """One k-way refinement pass of d_where (torch int32 CUDA tensor) on a
+        DeviceGraph.  Returns the number of vertices moved."""
+        mv = ctypes.c_int64(0)
+        cg = g_dev.as_cm()
+        _check(lib().cm_refine_kway(self._h, ctypes.byref(cg), int(nparts), ctypes.c_void_p(d_where.data_ptr()),
+                                    ctypes.byref(mv), _stream_ptr(stream)))
+        return int(mv.value)
+
+    def project(self, d_cmap, d_cwhere, d_where, stream=None):
+        _check(lib().cm_project(self._h, int(d_where.numel()), ctypes.c_void_p(d_cmap.data_ptr()),
+                                ctypes.c_void_p(d_cwhere.data_ptr()), ctypes.c_void_p(d_where.data_ptr()),
+                                _stream_ptr(stream)))
+
     def coarsen(self, g, coarsen_to, mode=MATCH_HEM, maxvwgt=0, shrink=0.75, max_levels=64, stream=None):
         """Coarsens a host Graph (uploaded inside the call) or a DeviceGraph."""
         p = cm_coarsen_params(int(coarsen_to), int(maxvwgt), int(mode), int(max_levels), float(shrink))

@@ -228,6 +228,67 @@ int cm_hierarchy_copy_level(const cm_hierarchy *h, int32_t level, cm_graph *out,
 int cm_hierarchy_read_level(const cm_hierarchy *h, int32_t level, int32_t *xadj, int32_t *adjncy,
                             int32_t *adjwgt, int32_t *vwgt);
 
+/* ---- partitioning: the tail of cuMetis_PartGraph ------------------------ */
+
+/* Initial partition of a host graph (normally the coarsest level) by
+ * multilevel recursive bisection, restating cuMetis_initialpartition
+ * (cuMetis.cu:3091) -> cuMetis_rbbisection (3046): per bisection a random
+ * heavy-edge coarsening to 200 vertices, 5 region-growing tries, 2-way
+ * balancing and Fiduccia-Mattheyses refinement (10 passes) projected back,
+ * then the split into two subgraphs.  `seed` seeds the C-library-compatible
+ * rand() stream the reference draws from (the reference never seeds it, which
+ * is seed 1).  part[nvtxs] gets part ids in [0, nparts); *objval the sum of
+ * the bisection cuts.  Host only; g's arrays are host pointers (vwgt/adjwgt
+ * may be NULL for unit weights). */
+int cm_initial_partition(const cm_graph *g, int32_t nparts, uint32_t seed, int32_t *part, int32_t *objval);
+
+/* One k-way refinement pass of partition d_where (device, n entries) on the
+ * device graph g_dev (cuMetis_uncoarsen, cuMetis.cu:3494-3514): boundary
+ * vertices move to their best-connected part, group by group per target part,
+ * within a 1.03 balance window.  *moves (may be NULL) = vertices moved. */
+int cm_refine_kway(cm_ctx *ctx, const cm_graph *g_dev, int32_t nparts, int32_t *d_where, int64_t *moves,
+                   void *stream);
+
+/* Projection d_where[v] = d_cwhere[d_cmap[v]] for v < n (cuMetis_kway_project,
+ * cuMetis.cu:3079). */
+int cm_project(cm_ctx *ctx, int32_t n, const int32_t *d_cmap, const int32_t *d_cwhere, int32_t *d_where,
+               void *stream);
+
+typedef struct cm_part_params {
+  int32_t seed;          /* initial-partition rand() seed (1 = the reference's stream) */
+  int32_t match_mode;    /* CM_MATCH_* for the coarsening                          */
+  int32_t refine_passes; /* refinement passes per level (the reference: 1)        */
+  int32_t coarsen_to;    /* 0: max(n / (20 log2 k), 30 k) (cuMetis.cu:3634)         */
+} cm_part_params;
+void cm_part_default_params(cm_part_params *p);
+
+typedef struct cm_part_stats {
+  double coarsen_ms, init_ms, uncoarsen_ms, total_ms;
+  int32_t levels;         /* graphs in the hierarchy, input included */
+  int32_t coarsest_nvtxs;
+  int32_t initial_cut;    /* objective of the initial partition      */
+  int64_t edge_cut;       /* final edge cut                          */
+  int64_t moves;          /* vertices moved by the refinement        */
+} cm_part_stats;
+
+/* k-way partition of a host graph: coarsen on the device, initial partition on
+ * the host, refinement and projection per level on the device; part[nvtxs]
+ * (caller-allocated) gets ids in [0, nparts).  Host arrays are read, never
+ * modified; vwgt/adjwgt may be NULL (unit weights).  tpwgts and ubvec are
+ * accepted and ignored, as in the reference (cuMetis.cu:370-394).  Unlike
+ * the reference, which leaves *objval = 0 (cu:3615), *objval is the final
+ * edge cut.  params/stats may be NULL. */
+int cm_part_graph(cm_ctx *ctx, int32_t nvtxs, const int32_t *xadj, const int32_t *adjncy, const int32_t *vwgt,
+                  const int32_t *adjwgt, int32_t nparts, const float *tpwgts, const float *ubvec, int32_t *objval,
+                  int32_t *part, const cm_part_params *params, cm_part_stats *stats);
+
+/* Drop-in for the reference's entry point, same parameter list
+ * (include/cuMetis.h:18-19, cuMetis.cu:3622): a context on the current device
+ * for the call.  Returns 1 on success (as the reference), 0 on failure with
+ * the message in cm_last_error() where the reference would exit. */
+int cuMetis_PartGraph(int *nvtxs, int *xadj, int *adjncy, int *vwgt, int *adjwgt, int *nparts, float *tpwgts,
+                      float *ubvec, int *objval, int *part);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,7 +58,7 @@ def ref():
         if path is None or not os.path.exists(path):
             return None
         _ref = ctypes.CDLL(path)
-        for name in ("ref_cpu_match_contract", "ref_cpu_contract"):
+        for name in ("ref_cpu_match_contract", "ref_cpu_contract", "ref_rbbisection"):
             getattr(_ref, name).restype = ctypes.c_int32
     return _ref
 
@@ -221,3 +221,82 @@ def match_from_cmap(cmap):
     a, b = order[same], order[same + 1]
     match[a], match[b] = b, a
     return match
+
+
+def ref_harness_rbbisection(g, nparts, seed):
+    """The reference's own initial partition (cuMetis_rbbisection,
+    cuMetis.cu:3046) of graph g into nparts, with its rand() stream seeded by
+    srand(seed).  Returns (part, objval)."""
+    R = ref()
+    if R is None:
+        raise RuntimeError("reference harness not built (reference tree absent)")
+    R.ref_srand(ctypes.c_uint(seed))
+    part = np.zeros(max(g.n, 1), np.int32)
+    obj = np.zeros(1, np.int32)
+    R.ref_rbbisection(ctypes.c_int32(g.n), _p(g.xadj), _p(g.adjncy), _p(g.vwgt), _p(g.adjwgt),
+                      ctypes.c_int32(nparts), _p(part), _p(obj))
+    return part[:g.n], int(obj[0])
+
+
+def _part_windows(tvwgt, k):
+    """Balance window of every part as Sum_maxmin_pwgts computes it
+    (cuMetis.cu:3424-3433) in single precision, tpwgts = (float)(1.0/k)."""
+    tp = np.float32(1.0 / k)
+    x = np.float32(tp * np.float32(tvwgt))
+    return int(np.float32(x * np.float32(1.03))), int(np.float32(x / np.float32(1.03)))
+
+
+def boundary_targets(g, where, k):
+    """Boundary flag and target part of every vertex (Find_real_bnd_info +
+    find_kayparams, cuMetis.cu:3236-3306): boundary when the weight to other
+    parts exceeds the weight to the own part; target = the first part id with
+    the largest connection if it beats the own part, else the own part."""
+    n = g.n
+    flag = np.zeros(n, bool)
+    target = where.copy()
+    for v in range(n):
+        lo, hi = g.xadj[v], g.xadj[v + 1]
+        nb = where[g.adjncy[lo:hi]]
+        w = g.adjwgt[lo:hi].astype(np.int64)
+        me = where[v]
+        mw = int(w[nb == me].sum())
+        ow = int(w[nb != me].sum())
+        if ow > mw:
+            flag[v] = True
+            acc = np.bincount(nb, weights=w, minlength=k).astype(np.int64)
+            mx = acc.max()
+            if mx > acc[me]:
+                target[v] = int(np.argmax(acc == mx))
+    return flag, target
+
+
+def refine_kway_model(g, where, k):
+    """One k-way refinement pass (cuMetis_uncoarsen, cuMetis.cu:3494-3514)
+    with the part groups run one after another in part order: boundary
+    vertices grouped by target part in vertex order; first the moves to a
+    higher part id, then to a lower one, each kept only if both parts stay in
+    their windows.  With two parts the GPU's concurrent part threads cannot
+    interleave (one group moves per phase), so this is exact for k = 2.
+    Returns (where, moves)."""
+    where = np.array(where, np.int32).copy()
+    vw = g.vwgt.astype(np.int64)
+    pw = np.bincount(where, weights=vw, minlength=k).astype(np.int64)
+    mx, mn = _part_windows(int(vw.sum()), k)
+    flag, target = boundary_targets(g, where, k)
+    groups = [[] for _ in range(k)]
+    for v in np.nonzero(flag)[0]:
+        groups[target[v]].append(int(v))
+    moves = 0
+    for up in (True, False):
+        for t in range(k):
+            for v in groups[t]:
+                me = int(where[v])
+                if (me >= t) if up else (me <= t):
+                    continue
+                w = int(vw[v])
+                if mn <= pw[t] + w <= mx and mn <= pw[me] - w <= mx:
+                    pw[t] += w
+                    pw[me] -= w
+                    where[v] = t
+                    moves += 1
+    return where, moves

@@ -9,6 +9,8 @@
 //   ref_cpu_match_contract  cuMetis_cpu_match (cuMetis.cu:830), which runs
 //                           cuMetis_cpu_create_cgraph (cu:737)
 //   ref_cpu_contract        cuMetis_cpu_create_cgraph on a caller's matching
+//   ref_rbbisection         cuMetis_rbbisection (cuMetis.cu:3046), the initial
+//                           partition by multilevel recursive bisection
 #define main cuMetis_reference_main
 #include "cuMetis.cu"
 #undef main
@@ -73,4 +75,24 @@ extern "C" int ref_cpu_contract(int n, const int *xadj, const int *adjncy, const
     if (i <= match[i]) g->cmap[i] = g->cmap[match[i]] = cn++;
   cuMetis_cpu_create_cgraph(a, g, cn, const_cast<int *>(match), 1);
   return export_coarse(g, cmap_out, cxadj, cvwgt, cadjncy, cadjwgt, cnedges);
+}
+
+// cuMetis_rbbisection frees the graph arrays it is given (cuMetis_free_graph
+// in cuMetis_mlevel_rbbisection, cu:3000), so it gets malloc'ed copies.
+extern "C" int ref_rbbisection(int n, const int *xadj, const int *adjncy, const int *vwgt, const int *adjwgt,
+                               int nparts, int *part, int *objval) {
+  int m = xadj[n];
+  int *x = (int *)malloc(sizeof(int) * (n + 1)), *a = (int *)malloc(sizeof(int) * (m > 0 ? m : 1));
+  int *vw = (int *)malloc(sizeof(int) * (n > 0 ? n : 1)), *aw = (int *)malloc(sizeof(int) * (m > 0 ? m : 1));
+  memcpy(x, xadj, sizeof(int) * (n + 1));
+  memcpy(a, adjncy, sizeof(int) * m);
+  memcpy(vw, vwgt, sizeof(int) * n);
+  memcpy(aw, adjwgt, sizeof(int) * m);
+  float ub = 1.03f;
+  float *tp = (float *)malloc(sizeof(float) * nparts);
+  for (int i = 0; i < nparts; ++i) tp[i] = 1.0f / nparts;
+  int nv = n, np_ = nparts;
+  cuMetis_rbbisection(&nv, x, a, vw, aw, &np_, tp, &ub, objval, part);
+  free(tp);
+  return 0;
 }

@@ -1,4 +1,5 @@
-"""Generates tests/golden/*.npz from the reference's own CPU coarsening.
+"""Generates tests/golden/*.npz from the reference's own CPU code: its CPU
+coarsening (one file per graph) and its initial partition (initpart.npz).
 
 Run here, where the reference tree is present (it builds the include-harness
 oracle/_ref/libref.so around the unmodified reference sources):
@@ -91,6 +92,35 @@ def ref_coarsen(g, threshold, seed, max_levels=32):
     return levels, cmaps, maxvwgt
 
 
+def two_grids():
+    """Two disconnected 20x20 grids (the bisection must restart its BFS)."""
+    g = cm.gen_grid2d(20, 20)
+    n, m = g.nvtxs, g.nedges
+    xadj = np.concatenate([g.xadj, g.xadj[1:] + m])
+    adj = np.concatenate([g.adjncy, g.adjncy + n])
+    return O.CSR(xadj, adj, np.ones(2 * m), np.ones(2 * n))
+
+
+# Initial-partition cases: graph, then (nparts, seed) pairs.  The reference's
+# cuMetis_rbbisection (cu:3046) runs with its rand() stream seeded by srand(seed).
+INITPART_KS = ((2, 1), (3, 1), (5, 4), (8, 1), (8, 2), (16, 3), (64, 1))
+
+
+def make_initpart(cases):
+    out = {}
+    for name, g in cases.items():
+        out[name + "_xadj"], out[name + "_adjncy"] = g.xadj, g.adjncy
+        out[name + "_adjwgt"], out[name + "_vwgt"] = g.adjwgt, g.vwgt
+        for k, seed in INITPART_KS:
+            part, obj = O.ref_harness_rbbisection(g, k, seed)
+            out["%s_k%d_s%d_part" % (name, k, seed)] = part
+            out["%s_k%d_s%d_obj" % (name, k, seed)] = np.int32(obj)
+    out["names"] = np.array(sorted(cases))
+    out["ks"] = np.array(INITPART_KS, np.int32)
+    np.savez_compressed(os.path.join(HERE, "initpart.npz"), **out)
+    print("initpart.npz", len(cases), "graphs")
+
+
 def main():
     if O.ref() is None:
         sys.exit("reference tree not found; golden fixtures can only be generated where it is present")
@@ -120,6 +150,11 @@ def main():
                 out[p + "L%d_cmap" % l] = cmap
             print(name, "seed", seed, "levels", [lg.n for lg in levels], "maxvwgt", maxvwgt)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+    make_initpart({"tri69": to_csr(cm.gen_tri_grid(69, 69)), "rmat10": to_csr(cm.gen_rmat(10, 16, seed=1)),
+                   "wgrid40": weighted_grid(40, 40), "rgg3000": to_csr(cm.gen_rgg(3000, 8.0, seed=3)),
+                   "two_grids": two_grids(),
+                   "3elt": read_mtx_symmetric(os.path.join(REF_TREE, "mtx", "3elt.mtx"))})
 
 
 if __name__ == "__main__":

@@ -118,7 +118,8 @@ def test_threshold_rule():
 def _declared_functions():
     text = open(os.path.join(ROOT, "include", "cm.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_ ]*?[\s\*]+(cm_[a-z0-9_]+)\s*\(", text, flags=re.M)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_ ]*?[\s\*]+((?:cm|cuMetis)_[A-Za-z0-9_]+)\s*\(", text,
+                       flags=re.M)
     return sorted(set(names))
 
 
@@ -126,6 +127,7 @@ def test_abi_exports_every_declared_symbol():
     lib = cm.lib()  # loads libcm.so (no device call)
     names = _declared_functions()
     assert len(names) >= 20
+    assert "cuMetis_PartGraph" in names and "cm_part_graph" in names
     out = subprocess.run(["nm", "-D", "--defined-only", cm.LIB_PATH], stdout=subprocess.PIPE, text=True).stdout
     exported = set(l.split()[-1] for l in out.splitlines() if l.strip())
     missing = [n for n in names if n not in exported]
@@ -141,3 +143,11 @@ def test_no_device_fails_loudly():
     with pytest.raises(cm.CMError) as e:
         cm.Context(0)
     assert e.value.code == cm.CM_ERR_UNSUPPORTED
+
+
+def test_cli_usage_without_arguments():
+    exe = os.path.join(os.path.dirname(cm.LIB_PATH), "cuMetis")
+    if not os.path.exists(exe):
+        cm.lib()
+    r = subprocess.run([exe], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr
