@@ -210,13 +210,157 @@ def cpu_baseline(g, k, budget_s=20.0):
                       (reps, dt)}
 
 
+def batch_graphs(count, seed=1):
+    """The batched workload: `count` random geometric graphs in the unit
+    square, n log-uniform in [1k, 200k], r = sqrt(8/(pi n)) (mean degree 8),
+    k uniform in {2, 4, ..., 64}; seeded."""
+    import cumetis_gb300 as cm
+    rng = np.random.default_rng(seed)
+    ns = np.exp(rng.uniform(np.log(1000), np.log(200000), count)).astype(np.int64)
+    ks = 2 * rng.integers(1, 33, count)
+    return [cm.gen_rgg(int(n), 8.0, seed=seed * 100003 + i) for i, n in enumerate(ns)], [int(k) for k in ks]
+
+
+def run_batch(args):
+    """Batched partitioning (cm_part_batch): partitions/s over the whole batch."""
+    import cumetis_gb300 as cm
+    t0 = time.perf_counter()
+    graphs, ks = batch_graphs(args.batch_graphs)
+    gen_s = time.perf_counter() - t0
+    warm = min(len(graphs), 32)
+    for _ in range(max(1, args.warmup // 3)):
+        cm.part_batch(graphs[:warm], ks[:warm], workers=args.workers)
+    clocks = ClockSampler(0)
+    clocks.start()
+    t1 = time.perf_counter()
+    _, cuts, st = cm.part_batch(graphs, ks, workers=args.workers)
+    dt = time.perf_counter() - t1
+    clk = clocks.stop()
+    n_sum = int(sum(g.nvtxs for g in graphs))
+    m_sum = int(sum(g.nedges for g in graphs))
+    imb = [float(np.bincount(p, minlength=k).max() * k / g.nvtxs) for g, p, k in
+           zip(graphs[:64], cm.part_batch(graphs[:64], ks[:64], workers=args.workers)[0], ks[:64])]
+    line = {"metric": "partitions/s", "value": len(graphs) / dt, "unit": "partitions/s", "n_gpus": 1, "steps": 1,
+            "warmup": max(1, args.warmup // 3), "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": "batch", "graphs": len(graphs), "sum_nvtxs": n_sum, "sum_nedges": m_sum,
+                       "description": "random geometric graphs, n log-uniform [1k,200k], mean degree 8, "
+                                      "k uniform in {2..64} even, unit weights",
+                       "workers": args.workers, "generation_s": gen_s, "engine_setup_ms": st["setup_ms"],
+                       "mean_phase_ms": {"coarsen": st["sum_coarsen_ms"] / len(graphs),
+                                         "initial_partition": st["sum_init_ms"] / len(graphs),
+                                         "refine_project": st["sum_uncoarsen_ms"] / len(graphs)}},
+            "edges_per_s": m_sum / dt, "mean_edge_cut": float(np.mean(cuts)),
+            "mean_imbalance_first64": float(np.mean(imb)), "clocks": clk, "gpu_launches": None,
+            "e2e": {"value": len(graphs) / dt, "unit": "partitions/s",
+                    "h2d_bytes_per_step": int(4 * (2 * n_sum + len(graphs) + 2 * m_sum)),
+                    "d2h_bytes_per_step": int(4 * n_sum)}}
+    print(json.dumps(line), flush=True)
+
+
+def serve_pool(seed=1, count=48):
+    """Request graphs of the served workload: half 3D 7-point grids with side
+    U[20,120], half R-MAT scale U{14..21} (edge factor 16, weights U[1,100])."""
+    import cumetis_gb300 as cm
+    rng = np.random.default_rng(seed)
+    pool = []
+    for i in range(count):
+        if i % 2 == 0:
+            s = int(rng.integers(20, 121))
+            pool.append(("grid3d_%d" % s, cm.gen_grid3d(s, s, s)))
+        else:
+            sc = int(rng.integers(14, 22))
+            pool.append(("rmat%d" % sc, cm.gen_rmat(sc, 16, 0.57, 0.19, 0.19, seed * 1000 + i, 1, 100)))
+    return pool
+
+
+def run_serve(args):
+    """Served partitioning (cm_engine): Poisson arrivals at --rate requests/s
+    for --duration seconds, each a random pool graph with k uniform in
+    {8..256}.  Submissions beyond --max-queue waiting jobs are rejected; after
+    the window the engine drains for at most --drain seconds, then drops what
+    has not started.  Reports completions/s and latency percentiles of the
+    completed requests."""
+    import cumetis_gb300 as cm
+    rng = np.random.default_rng(7)
+    t0 = time.perf_counter()
+    pool = serve_pool(count=args.serve_pool)
+    gen_s = time.perf_counter() - t0
+    max_n = max(g.nvtxs for _, g in pool)
+    max_m = max(g.nedges for _, g in pool)
+    eng = cm.Engine(0, workers=args.workers, hbm_budget_bytes=int(args.hbm_budget_gb * 2**30),
+                    max_queue=args.max_queue, reserve_nvtxs=max_n, reserve_nedges=max_m)
+    for _, g in pool[:4]:  # warm-up
+        eng.wait(eng.submit(g, 16))
+    eng.stats(reset=True)
+    clocks = ClockSampler(0)
+    clocks.start()
+    jobs, rejected = [], 0
+    t_start = time.perf_counter()
+    t_next = t_start
+    while True:
+        now = time.perf_counter()
+        if now - t_start >= args.duration:
+            break
+        if now < t_next:
+            time.sleep(min(t_next - now, 0.001))
+            continue
+        _, g = pool[int(rng.integers(0, len(pool)))]
+        try:
+            jobs.append(eng.submit(g, int(rng.integers(8, 257))))
+        except cm.CMError as e:
+            if e.code != cm.CM_ERR_LIMIT:
+                raise
+            rejected += 1
+        t_next += rng.exponential(1.0 / args.rate)
+    t_window = time.perf_counter()
+    deadline = t_window + args.drain
+    lat, unfinished = [], 0
+    for j in jobs:
+        while not eng.poll(j) and time.perf_counter() < deadline:
+            time.sleep(0.001)
+        if eng.poll(j):
+            lat.append(eng.wait(j)[2]["latency_ms"])
+        else:
+            unfinished += 1
+    t_end = time.perf_counter()
+    clk = clocks.stop()
+    eng.close()  # drops jobs that never started
+    lat = np.sort(np.array(lat))
+    done = len(lat)
+    line = {"metric": "partitions/s", "value": done / (t_end - t_start), "unit": "partitions/s", "n_gpus": 1,
+            "steps": done, "warmup": 4, "ms_per_step": (t_end - t_start) * 1e3 / max(done, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": "serve", "offered_rate": args.rate, "duration_s": args.duration,
+                       "drain_s": args.drain, "max_queue": args.max_queue, "pool": len(pool),
+                       "pool_generation_s": gen_s, "workers": args.workers, "hbm_budget_gb": args.hbm_budget_gb,
+                       "description": "Poisson arrivals; 50% 3D 7-point grids side U[20,120], 50% R-MAT "
+                                      "s14-21 (ef 16, weights U[1,100]); k uniform in {8..256}"},
+            "submitted": len(jobs), "rejected": rejected, "completed": done, "unfinished_dropped": unfinished,
+            "latency_ms": {"p50": float(np.percentile(lat, 50)) if done else None,
+                           "p99": float(np.percentile(lat, 99)) if done else None,
+                           "max": float(lat[-1]) if done else None},
+            "clocks": clk, "gpu_launches": None,
+            "e2e": {"value": done / (t_end - t_start), "unit": "partitions/s", "h2d_bytes_per_step": None,
+                    "d2h_bytes_per_step": None}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="rmat22", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="rmat22", choices=sorted(WORKLOADS) + ["batch", "serve"])
+    ap.add_argument("--workers", type=int, default=8, help="batch/serve: worker threads (one context each)")
+    ap.add_argument("--batch-graphs", type=int, default=4096)
+    ap.add_argument("--rate", type=float, default=2000.0, help="serve: offered requests/s")
+    ap.add_argument("--duration", type=float, default=10.0, help="serve: arrival window in seconds")
+    ap.add_argument("--serve-pool", type=int, default=48, help="serve: distinct request graphs")
+    ap.add_argument("--hbm-budget-gb", type=float, default=200.0, help="serve: admission budget")
+    ap.add_argument("--max-queue", type=int, default=64, help="serve: waiting jobs before submissions are rejected")
+    ap.add_argument("--drain", type=float, default=10.0, help="serve: seconds to wait for admitted jobs")
     ap.add_argument("--mode", type=int, default=0, help="matching mode (0 = heaviest edge, ties to lower id)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) measurement")
@@ -227,6 +371,10 @@ def main():
         run_reference(args, ws, rank)
         barrier(ws)
         return
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload == "serve":
+        return run_serve(args)
 
     import torch
     import cumetis_gb300 as cm

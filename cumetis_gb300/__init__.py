@@ -51,6 +51,17 @@ class cm_part_stats(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class cm_job_info(ctypes.Structure):
+    _fields_ = [("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("stats", cm_part_stats), ("status", ctypes.c_int32)]
+
+
+class cm_batch_stats(ctypes.Structure):
+    _fields_ = [("setup_ms", ctypes.c_double), ("run_ms", ctypes.c_double), ("graphs", ctypes.c_int32),
+                ("sum_nedges", ctypes.c_int64), ("sum_cut", ctypes.c_int64), ("sum_coarsen_ms", ctypes.c_double),
+                ("sum_init_ms", ctypes.c_double), ("sum_uncoarsen_ms", ctypes.c_double)]
+
+
 _lib = None
 
 
@@ -115,6 +126,16 @@ def _declare(L):
         "cm_part_graph": (c_int, [c_vp, c_i32, _I32P, _I32P, _I32P, _I32P, c_i32, c_vp, c_vp, _I32P, _I32P,
                                   ctypes.POINTER(cm_part_params), ctypes.POINTER(cm_part_stats)]),
         "cuMetis_PartGraph": (c_int, [_I32P, _I32P, _I32P, _I32P, _I32P, _I32P, c_vp, c_vp, _I32P, _I32P]),
+        "cm_ctx_stream": (c_vp, [c_vp]),
+        "cm_engine_create": (c_int, [c_int, c_i32, c_i64, c_i32, c_i64, c_i64, ctypes.POINTER(c_vp)]),
+        "cm_engine_poll": (c_int, [c_vp, c_i64, _I32P]),
+        "cm_engine_destroy": (None, [c_vp]),
+        "cm_engine_submit": (c_int, [c_vp, G, c_i32, ctypes.POINTER(cm_part_params), _I32P, ctypes.POINTER(c_i64)]),
+        "cm_engine_wait": (c_int, [c_vp, c_i64, _I32P, ctypes.POINTER(cm_job_info)]),
+        "cm_engine_stats": (c_int, [c_vp, ctypes.POINTER(c_i64), ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_double), c_int]),
+        "cm_part_batch": (c_int, [c_int, c_i32, c_i32, G, _I32P, ctypes.POINTER(_I32P), _I32P,
+                                  ctypes.POINTER(cm_part_params), ctypes.POINTER(cm_batch_stats)]),
     }
     for name, (res, args) in list(sigs.items()) + list(optional.items()):
         fn = getattr(L, name, None)
@@ -275,4 +296,5 @@ def maxvwgt_rule(tvwgt, threshold):
     return int(1.5 * tvwgt / threshold)
 
 
+from .engine import Engine, part_batch  # noqa: E402,F401
 from .device import Context, Hierarchy  # noqa: E402  (device side, needs libcm's CUDA entry points)

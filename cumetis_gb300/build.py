@@ -20,7 +20,7 @@ CLI = os.path.join(HERE, "cuMetis")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["cm_ctx.cu", "cm_match.cu", "cm_cmap.cu", "cm_contract.cu", "cm_refine.cu"]
-CPP_SOURCES = ["cm_graph.cpp", "cm_initpart.cpp"]
+CPP_SOURCES = ["cm_graph.cpp", "cm_initpart.cpp", "cm_engine.cpp"]
 CLI_SOURCES = ["cm_cli.cpp"]
 
 
@@ -78,7 +78,8 @@ def build(force=False, bounds_check=False, verbose=False):
         with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
             logs = list(ex.map(_compile, jobs))
     if jobs or not os.path.exists(LIB):
-        subprocess.check_call([nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-Xcompiler", "-fopenmp", "-lgomp"])
+        subprocess.check_call([nvcc, "-shared", *ARCH, "-o", LIB, *objs, "-Xcompiler", "-fopenmp", "-lgomp",
+                               "-lpthread"])
     cli_srcs = [os.path.join(CSRC, f) for f in CLI_SOURCES if os.path.exists(os.path.join(CSRC, f))]
     if cli_srcs and (force or jobs or not os.path.exists(CLI) or _stale(CLI, cli_srcs[0], deps + [LIB])):
         subprocess.check_call(["g++", "-std=c++17", "-O2", "-I" + INCLUDE, *cli_srcs, "-o", CLI, "-L" + HERE, "-lcm",

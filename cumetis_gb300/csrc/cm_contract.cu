@@ -29,6 +29,8 @@
 //                   merged pairwise (merge path, all blocks cooperating, one
 //                   grid barrier per pass) and deduplicated.  Their unique
 //                   entries are copied out beside the emit pass.
+#include <algorithm>
+
 #include "cm_ctx.h"
 #include "cm_sort.cuh"
 
@@ -553,8 +555,10 @@ __device__ __forceinline__ int merge_path_g(const int2 *A, int alen, const int2 
   return lo;
 }
 
-// All long rows' merge passes in one cooperative launch: pass p merges run
-// pairs of width kChunk << p.  A block produces one kChunk-sized block of
+// One merge pass per launch: pass p merges run pairs of width kChunk << p
+// (launches beyond the longest row's last pass return at once; the host
+// launches the most passes a graph of m entries can need).  A block produces
+// one kChunk-sized block of
 // output: two threads find where it starts and ends in the two runs (merge
 // path over global memory), the block loads both windows into shared memory,
 // every thread merges kMergePer outputs there, and the block stores the
@@ -568,13 +572,13 @@ struct MergeSmem {
 };
 
 __global__ void __launch_bounds__(kMergeThreads)
-k_long_merge(const int *__restrict__ long_list, const int *__restrict__ chunk_row, const int *__restrict__ eoff,
-             const unsigned long long *long_ctr, int2 *stage0, int2 *stage1, DevStatus *st) {
+k_long_merge(int p, const int *__restrict__ long_list, const int *__restrict__ chunk_row, const int *__restrict__ eoff,
+             const unsigned long long *long_ctr, int2 *stage0, int2 *stage1, const DevStatus *st) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MergeSmem &S = *reinterpret_cast<MergeSmem *>(smem_raw);
   const int nchunks = (int)(*long_ctr & 0xffffffffu);
-  const int npass = merge_passes(st->max_row);
-  for (int p = 0; p < npass; ++p) {
+  if (p >= merge_passes(st->max_row)) return;
+  {
     const long long width = (long long)kChunk << p;
     const int2 *src = (p & 1) ? stage1 : stage0;
     int2 *dst = (p & 1) ? stage0 : stage1;
@@ -632,7 +636,6 @@ k_long_merge(const int *__restrict__ long_list, const int *__restrict__ chunk_ro
       for (int t = threadIdx.x; t < nout; t += kMergeThreads) o[t] = unpack_entry(S.out[padk<unsigned long long>(t)]);
       __syncthreads();
     }
-    if (p + 1 < npass && !grid_barrier(st, gridDim.x)) return;
   }
 }
 
@@ -736,6 +739,10 @@ __global__ void k_long_copy(const int *__restrict__ long_list, const int *__rest
 
 }  // namespace
 
+// Grid of a kernel that loops over at most `items` work items: no more blocks
+// than items (at least one), at most `cap`.
+static unsigned grid_for(int64_t cap, int64_t items) { return (unsigned)std::max<int64_t>(1, std::min(cap, items)); }
+
 size_t contract_ws_bytes(int64_t n, int64_t m) {
   const int64_t ntiles = (n + m) / kTileDiag + 2;
   const int64_t nchunks = m / kChunk + m / kLongThr + 2;
@@ -814,32 +821,30 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   stage_begin(ctx, s);
   cudaEventRecord(ctx->fork_ev, s);
   for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(ctx->aux[i], ctx->fork_ev, 0);
-  k_mid_rows<256, 2 * kLongThr><<<sms * 4, 256, sizeof(MidSmem<2 * kLongThr>), ctx->aux[0]>>>(
+  k_mid_rows<256, 2 * kLongThr><<<grid_for(sms * 4, m / (kLongThr + 1)), 256, sizeof(MidSmem<2 * kLongThr>), ctx->aux[0]>>>(
       fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list, mid_ctr + 0, stage1, ucount);
-  k_mid_rows<512, 4 * kLongThr><<<sms * 2, 512, sizeof(MidSmem<4 * kLongThr>), ctx->aux[1]>>>(
+  k_mid_rows<512, 4 * kLongThr><<<grid_for(sms * 2, m / (2 * kLongThr + 1)), 512, sizeof(MidSmem<4 * kLongThr>), ctx->aux[1]>>>(
       fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + mid_cap, mid_ctr + 1, stage1, ucount);
-  k_mid_rows<1024, kChunk><<<sms, 1024, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
+  k_mid_rows<1024, kChunk><<<grid_for(sms, m / (4 * kLongThr + 1)), 1024, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
       fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + 2 * mid_cap, mid_ctr + 2, stage1, ucount);
-  k_long_sort<<<sms, kChunkThreads, sizeof(ChunkSmem), ctx->aux[2]>>>(
+  // Grids of the chunked-row kernels scale with the most chunks the graph can
+  // have (m / kChunk), so small graphs do not claim every SM.
+  const int long_grid = (int)std::min<int64_t>(sms, m / kChunk / 4 + 1);
+  k_long_sort<<<long_grid, kChunkThreads, sizeof(ChunkSmem), ctx->aux[2]>>>(
       fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, long_list, chunk_row, ctr, stage0, ucount);
   ctx->launches += 4;
   {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_long_merge, kMergeThreads, sizeof(MergeSmem));
-    int grid = sms * (per_sm > 0 ? per_sm : 1);
-    const int *a0 = long_list;
-    const int *a1 = chunk_row;
-    const int *a2 = eoff;
-    const unsigned long long *a3 = ctr;
-    int2 *a4 = stage0, *a5 = stage1;
-    DevStatus *a6 = st;
-    void *args[] = {(void *)&a0, (void *)&a1, (void *)&a2, (void *)&a3, (void *)&a4, (void *)&a5, (void *)&a6};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_long_merge, dim3(grid), dim3(kMergeThreads), args,
-                                                sizeof(MergeSmem), ctx->aux[2]);
-    if (e != cudaSuccess) return cuda_status(e, "contract: long-row merge launch");
-    ctx->launches++;
+    // Passes a row of at most m entries can need; each is a plain launch.
+    int max_pass = 0;
+    for (int64_t w = kChunk; w < m; w <<= 1) ++max_pass;
+    const int merge_grid = (int)std::min<int64_t>((int64_t)sms * 2, m / kChunk + 1);
+    for (int p = 0; p < max_pass; ++p) {
+      k_long_merge<<<merge_grid, kMergeThreads, sizeof(MergeSmem), ctx->aux[2]>>>(p, long_list, chunk_row, eoff, ctr,
+                                                                                  stage0, stage1, st);
+      ctx->launches++;
+    }
   }
-  k_long_dedup<<<sms * 4, kDedupThreads, 0, ctx->aux[2]>>>(long_list, chunk_row, eoff, ctr, stage0, stage1, stage0,
+  k_long_dedup<<<long_grid * 4, kDedupThreads, 0, ctx->aux[2]>>>(long_list, chunk_row, eoff, ctr, stage0, stage1, stage0,
                                                             stage1, chunk_cnt, ucount);
   ctx->launches++;
   for (int i = 0; i < 3; ++i) cudaEventRecord(ctx->join_ev[i], ctx->aux[i]);
@@ -865,7 +870,7 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   stage_begin(ctx, s);
   cudaEventRecord(ctx->fork_ev, s);
   cudaStreamWaitEvent(ctx->aux[0], ctx->fork_ev, 0);
-  k_long_copy<<<sms * 4, 256, 0, ctx->aux[0]>>>(long_list, chunk_row, eoff, ctr, mid_list, mid_ctr, (int)mid_cap,
+  k_long_copy<<<grid_for(sms * 4, m / kLongThr), 256, 0, ctx->aux[0]>>>(long_list, chunk_row, eoff, ctr, mid_list, mid_ctr, (int)mid_cap,
                                                  stage0, stage1, chunk_cnt, ucount, coarse->xadj, coarse->adjncy,
                                                  coarse->adjwgt);
   cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);

@@ -161,6 +161,7 @@ extern "C" int cm_ctx_create(int device, cm_ctx **out) {
   if (!rc) rc = cuda_status(cudaMemset(ctx->d_status, 0, sizeof(DevStatus)), "status init");
   if (!rc) rc = cuda_status(cudaMallocHost(&ctx->h_status, sizeof(DevStatus)), "pinned status alloc");
   if (!rc) rc = cuda_status(cudaMallocHost(&ctx->h_small, 64), "pinned readback alloc");
+  if (!rc) rc = cuda_status(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "context stream");
   for (int i = 0; i < 3 && !rc; ++i) {
     rc = cuda_status(cudaStreamCreateWithFlags(&ctx->aux[i], cudaStreamNonBlocking), "aux stream");
     if (!rc) rc = cuda_status(cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming), "aux event");
@@ -198,8 +199,11 @@ extern "C" void cm_ctx_destroy(cm_ctx *ctx) {
     if (ctx->join_ev[i]) cudaEventDestroy(ctx->join_ev[i]);
   }
   if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
+
+extern "C" void *cm_ctx_stream(const cm_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
 extern "C" int cm_ctx_reserve(cm_ctx *ctx, int64_t nvtxs, int64_t nedges) {
   if (!ctx || nvtxs < 0 || nedges < 0) return cm_fail(CM_ERR_INVALID, "cm_ctx_reserve: bad arguments");

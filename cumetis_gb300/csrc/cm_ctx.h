@@ -27,6 +27,9 @@ struct cm_ctx {
   std::vector<Pending> pending;
   double stage_ms[CM_STAGE_COUNT] = {0};
   cudaEvent_t ev_open = nullptr;
+  // the context's own stream (non-blocking), used by calls without a stream
+  // argument (cm_part_graph)
+  cudaStream_t stream = nullptr;
   // internal streams/events for concurrent contraction stages
   cudaStream_t aux[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t fork_ev = nullptr, join_ev[3] = {nullptr, nullptr, nullptr};

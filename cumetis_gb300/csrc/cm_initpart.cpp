@@ -558,6 +558,42 @@ void two_way_refine(Admin &a, HGraph &g, const float *ntpwgts, int iteration_num
   }
 }
 
+// Untraversed vertices as a Fenwick tree of 0/1 flags: kth(k) is the k-th
+// (0-based) untraversed vertex in id order, the vertex the reference finds by
+// a linear scan (cu:2588-2598) -- the same choice in O(log n), so graphs with
+// many components (isolated vertices restart the search once each) do not
+// turn the region growing quadratic.
+class Untraversed {
+ public:
+  explicit Untraversed(int n) : n_(n), t_(n + 1, 0), log_(1) {
+    for (int i = 1; i <= n; ++i) {
+      t_[i] += 1;
+      const int j = i + (i & -i);
+      if (j <= n) t_[j] += t_[i];
+    }
+    while ((1 << log_) <= n) ++log_;
+  }
+  void take(int v) {
+    for (int i = v + 1; i <= n_; i += i & -i) t_[i] -= 1;
+  }
+  int kth(int k) const {  // smallest v with (untraversed in [0, v]) == k + 1
+    int pos = 0, rem = k + 1;
+    for (int b = log_; b >= 0; --b) {
+      const int nx = pos + (1 << b);
+      if (nx <= n_ && t_[nx] < rem) {
+        pos = nx;
+        rem -= t_[nx];
+      }
+    }
+    return pos;  // 0-based vertex id
+  }
+
+ private:
+  int n_;
+  std::vector<int> t_;
+  int log_;
+};
+
 // Breadth-first region growing from random seeds, niparts tries, each
 // balanced and refined; the best cut wins (cuMetis_cpu_growbisection,
 // cu:2536-2660).
@@ -576,22 +612,18 @@ void grow_bisection(Admin &a, HGraph &g, const float *ntpwgts, int niparts) {
     int pw[2];
     pw[1] = g.tvwgt;
     pw[0] = 0;
+    Untraversed un(n);
     queue[0] = a.randinrange(n);
     tra[queue[0]] = 1;
+    un.take(queue[0]);
     int first = 0, last = 1, nleft = n - 1, dd = 0;
     for (;;) {
       if (first == last) {
         if (nleft == 0 || dd) break;
-        int k = a.randinrange(nleft);
-        int i;
-        for (i = 0; i < n; ++i) {
-          if (tra[i] == 0) {
-            if (k == 0) break;
-            k--;
-          }
-        }
+        const int i = un.kth(a.randinrange(nleft));
         queue[0] = i;
         tra[i] = 1;
+        un.take(i);
         first = 0;
         last = 1;
         nleft--;
@@ -611,6 +643,7 @@ void grow_bisection(Admin &a, HGraph &g, const float *ntpwgts, int niparts) {
         if (tra[k] == 0) {
           queue[last++] = k;
           tra[k] = 1;
+          un.take(k);
           nleft--;
         }
       }

@@ -29,12 +29,15 @@
 // neighbour answers both "matched?" and the weight cap.
 #include <climits>
 
+#include <algorithm>
+
 #include "cm_ctx.h"
 
 namespace cm {
 namespace {
 
 constexpr int kMatchThreads = 1024;
+constexpr int64_t kWorkPerBlock = 32768;  // vertices + entries per block of the matching grid
 constexpr int kSerialDeg = 16;   // rows scanned by one lane
 constexpr int kChunk = 256;      // entries per warp work item
 constexpr int kTop = 4;          // cached candidates per vertex
@@ -604,7 +607,10 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
   const void *fn = mode == CM_MATCH_HEM_HASH ? (const void *)k_match<true> : (const void *)k_match<false>;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kMatchThreads, 0);
   if (per_sm < 1) return cm_fail(CM_ERR_CUDA, "cm_match: kernel cannot be resident");
-  const int grid = ctx->num_sms * per_sm;
+  // Small graphs take a few SMs, so that kernels of other contexts (other
+  // streams) can run beside this one; the kernel is grid-size agnostic.
+  const int64_t want = (n + g->nedges) / kWorkPerBlock + 1;
+  const int grid = (int)std::min<int64_t>((int64_t)ctx->num_sms * per_sm, want);
   void *args[] = {(void *)&a};
   stage_begin(ctx, s);
   cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kMatchThreads), args, 0, s);

@@ -478,7 +478,7 @@ extern "C" int cm_part_graph(cm_ctx *ctx, int32_t nvtxs, const int32_t *xadj, co
   }
   int rc = set_device(ctx);
   if (rc) return rc;
-  cudaStream_t s = nullptr;
+  cudaStream_t s = ctx->stream;  // the context's own stream: concurrent contexts overlap
   const int64_t m = xadj[nvtxs];
   // Unit weights where the caller passes none (cuMetis_set_graph, cu:479-503).
   std::vector<int32_t> uv, ue;

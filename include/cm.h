@@ -115,6 +115,9 @@ const char *cm_last_error(void);
  * recorded since the last check (CM_ERR_LIMIT for a timed-out device wait,
  * CM_ERR_INVALID for an invalid matching), clearing it. */
 int cm_ctx_sync(cm_ctx *ctx, void *stream);
+/* The context's own non-blocking stream (a cudaStream_t), used by entry
+ * points without a stream argument (cm_part_graph). */
+void *cm_ctx_stream(const cm_ctx *ctx);
 /* Number of kernels this context has launched since creation. */
 int64_t cm_ctx_launch_count(const cm_ctx *ctx);
 
@@ -288,6 +291,53 @@ int cm_part_graph(cm_ctx *ctx, int32_t nvtxs, const int32_t *xadj, const int32_t
  * the message in cm_last_error() where the reference would exit. */
 int cuMetis_PartGraph(int *nvtxs, int *xadj, int *adjncy, int *vwgt, int *adjwgt, int *nparts, float *tpwgts,
                       float *ubvec, int *objval, int *part);
+
+/* ---- many graphs: batched and served partitioning ----------------------- */
+/* No counterpart in the reference (one graph per process).  An engine is a
+ * pool of worker threads on one device, each with its own context and
+ * stream; a worker runs cm_part_graph for one job at a time, so jobs overlap
+ * on the GPU and their host steps run in parallel.  A job is admitted while
+ * the estimated device memory of running jobs stays within hbm_budget_bytes
+ * (<= 0: no limit; a job larger than the budget runs alone).  reserve_* size
+ * every worker's workspace up front (0: grow on demand, which synchronises
+ * the device).  Host arrays of a submitted graph and its part buffer must
+ * stay valid until cm_engine_wait returns for the job (or the engine is
+ * destroyed). */
+typedef struct cm_engine cm_engine;
+typedef struct cm_job_info {
+  double queue_ms;     /* submit -> start  */
+  double run_ms;       /* start -> end     */
+  double latency_ms;   /* submit -> end    */
+  cm_part_stats stats;
+  int32_t status;      /* CM_OK or the job's error code */
+} cm_job_info;
+/* max_queue > 0 bounds the jobs waiting to start: cm_engine_submit then
+ * returns CM_ERR_LIMIT when it is full. */
+int  cm_engine_create(int device, int32_t nworkers, int64_t hbm_budget_bytes, int32_t max_queue,
+                      int64_t reserve_nvtxs, int64_t reserve_nedges, cm_engine **out);
+/* Lets running jobs finish, drops jobs not started, frees the engine. */
+void cm_engine_destroy(cm_engine *e);
+int  cm_engine_submit(cm_engine *e, const cm_graph *g_host, int32_t nparts, const cm_part_params *params,
+                      int32_t *part, int64_t *job_id);
+/* *done = 1 once the job has finished (non-blocking). */
+int  cm_engine_poll(cm_engine *e, int64_t job_id, int32_t *done);
+/* Blocks until the job is done; returns its status (the job is forgotten). */
+int  cm_engine_wait(cm_engine *e, int64_t job_id, int32_t *objval, cm_job_info *info);
+/* Jobs completed and latency percentiles (submit -> end) since the last reset. */
+int  cm_engine_stats(cm_engine *e, int64_t *completed, double *p50_ms, double *p99_ms, int reset);
+
+typedef struct cm_batch_stats {
+  double setup_ms;     /* engine and workspace creation */
+  double run_ms;       /* first submit -> last result   */
+  int32_t graphs;
+  int64_t sum_nedges;
+  int64_t sum_cut;
+  double sum_coarsen_ms, sum_init_ms, sum_uncoarsen_ms;  /* per-job phase times, summed */
+} cm_batch_stats;
+/* Partitions nbatch host graphs (graph i into nparts[i] parts, result in
+ * parts[i]) with nworkers workers; objvals[i] (may be NULL) = edge cuts. */
+int cm_part_batch(int device, int32_t nworkers, int32_t nbatch, const cm_graph *graphs, const int32_t *nparts,
+                  int32_t *const *parts, int32_t *objvals, const cm_part_params *params, cm_batch_stats *stats);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,65 @@
+"""Batched and served partitioning (cm_part_batch, cm_engine_*) on the GPU.
+Two-part partitions are deterministic end to end, so every job of a batch or
+an engine must equal the single-graph call on the same graph."""
+import numpy as np
+import pytest
+
+import cumetis_gb300 as cm
+
+pytestmark = pytest.mark.gpu
+
+
+def _graphs():
+    gs = [cm.gen_rgg(int(n), 8.0, seed=int(s)) for n, s in ((1000, 1), (3000, 2), (8000, 3), (20000, 4),
+                                                             (1500, 5), (50000, 6))]
+    gs += [cm.gen_grid2d(40, 30), cm.gen_grid3d(12, 12, 12), cm.gen_tri_grid(50, 50), cm.gen_rmat(11, 16, seed=3)]
+    return gs
+
+
+def test_batch_two_parts_matches_single_calls(ctx):
+    gs = _graphs()
+    parts, cuts, st = cm.part_batch(gs, 2, workers=4)
+    assert st["graphs"] == len(gs) and st["sum_cut"] == int(cuts.sum())
+    for g, p, c in zip(gs, parts, cuts):
+        want, wcut, _ = ctx.part_graph(g, 2, seed=1)
+        np.testing.assert_array_equal(p, want)
+        assert c == wcut == g.edge_cut(p)
+
+
+def test_batch_mixed_k_valid():
+    gs = _graphs()
+    ks = [2, 4, 8, 16, 32, 64, 3, 5, 7, 12]
+    parts, cuts, _ = cm.part_batch(gs, ks, workers=8)
+    for g, k, p, c in zip(gs, ks, parts, cuts):
+        assert p.min() >= 0 and p.max() < k
+        assert c == g.edge_cut(p)
+        pw = np.bincount(p, weights=g.vwgt, minlength=k)
+        assert pw.max() * k / g.vwgt.sum() < 1.2
+
+
+def test_engine_budget_serialises_but_completes(ctx):
+    gs = _graphs()[:6]
+    e = cm.Engine(0, workers=4, hbm_budget_bytes=1)  # every job exceeds the budget: one at a time
+    jobs = [e.submit(g, 2) for g in gs]
+    for g, j in zip(gs, jobs):
+        p, c, info = e.wait(j)
+        want, wcut, _ = ctx.part_graph(g, 2, seed=1)
+        np.testing.assert_array_equal(p, want)
+        assert info["latency_ms"] >= info["run_ms"] >= 0
+    s = e.stats()
+    assert s["completed"] == len(gs) and 0 < s["p50_ms"] <= s["p99_ms"]
+    e.close()
+
+
+def test_engine_many_jobs_and_errors():
+    e = cm.Engine(0, workers=8)
+    gs = [cm.gen_rgg(2000 + 100 * i, 8.0, seed=i) for i in range(48)]
+    jobs = [e.submit(g, 2 + i % 7) for i, g in enumerate(gs)]
+    for i, (g, j) in enumerate(zip(gs, jobs)):
+        p, c, _ = e.wait(j)
+        assert p.max() < 2 + i % 7 and c == g.edge_cut(p)
+    with pytest.raises(cm.CMError):
+        e.wait(cm.engine.Job(e, 123456, gs[0], np.zeros(1, np.int32)))
+    with pytest.raises(cm.CMError):
+        e.submit(gs[0], 0)
+    e.close()

@@ -151,3 +151,12 @@ def test_cli_usage_without_arguments():
         cm.lib()
     r = subprocess.run([exe], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
     assert r.returncode == 2 and "usage" in r.stderr
+
+
+def test_engine_without_device_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(cm.CMError) as e:
+        cm.Engine(0, workers=2)
+    assert e.value.code == cm.CM_ERR_UNSUPPORTED
