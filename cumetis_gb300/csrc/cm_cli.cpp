@@ -2,7 +2,7 @@
 // top of the C ABI only.
 //
 //   cuMetis <graph> <k> [--seed S] [--device D] [--coarsen-to N] [--passes P]
-//                       [--hash-ties] [--no-write]
+//                       [--lex-ties] [--no-write]
 //
 // Reads a METIS .graph file, partitions it into k parts (cm_part_graph),
 // prints the reference's report lines (timings, edge cut) plus the imbalance,
@@ -19,7 +19,7 @@
 
 static int usage(const char *argv0) {
   std::fprintf(stderr,
-               "usage: %s <graph> <k> [--seed S] [--device D] [--coarsen-to N] [--passes P] [--hash-ties] "
+               "usage: %s <graph> <k> [--seed S] [--device D] [--coarsen-to N] [--passes P] [--lex-ties] "
                "[--no-write]\n",
                argv0);
   return 2;
@@ -39,7 +39,7 @@ int main(int argc, char **argv) {
     else if (!std::strcmp(argv[i], "--device") && i + 1 < argc) device = std::atoi(argv[++i]);
     else if (!std::strcmp(argv[i], "--coarsen-to") && i + 1 < argc) P.coarsen_to = std::atoi(argv[++i]);
     else if (!std::strcmp(argv[i], "--passes") && i + 1 < argc) P.refine_passes = std::atoi(argv[++i]);
-    else if (!std::strcmp(argv[i], "--hash-ties")) P.match_mode = CM_MATCH_HEM_HASH;
+    else if (!std::strcmp(argv[i], "--lex-ties")) P.match_mode = CM_MATCH_HEM;
     else if (!std::strcmp(argv[i], "--no-write")) write = false;
     else return usage(argv[0]);
   }

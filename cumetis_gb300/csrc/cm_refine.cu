@@ -452,7 +452,10 @@ extern "C" int cm_project(cm_ctx *ctx, int32_t n, const int32_t *d_cmap, const i
 extern "C" void cm_part_default_params(cm_part_params *p) {
   if (!p) return;
   p->seed = 1;
-  p->match_mode = CM_MATCH_HEM;
+  // Hash-ordered ties: on unit-weight meshes the lowest-id order chains the
+  // handshakes (hundreds of rounds per level) while hashed ties settle in a
+  // few; both give deterministic heavy-edge matchings.
+  p->match_mode = CM_MATCH_HEM_HASH;
   p->refine_passes = 1;
   p->coarsen_to = 0;
 }

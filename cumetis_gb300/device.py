@@ -5,7 +5,8 @@ import ctypes
 
 import numpy as np
 
-from . import (CM_OK, CMError, Graph, DeviceGraph, cm_coarsen_params, cm_graph, lib, _check, MATCH_HEM)
+from . import (CM_OK, CMError, Graph, DeviceGraph, cm_coarsen_params, cm_graph, lib, _check, MATCH_HEM,
+               MATCH_HEM_HASH)
 
 
 def _torch():
@@ -132,7 +133,7 @@ class Context:
         return DeviceGraph(cx[:cn + 1], ca[:cm_], cw[:cm_], cv[:cn]), cmap[:n]
 
     # ---- multilevel -------------------------------------------------------
-    def part_graph(self, g, nparts, seed=1, mode=MATCH_HEM, refine_passes=1, coarsen_to=0):
+    def part_graph(self, g, nparts, seed=1, mode=MATCH_HEM_HASH, refine_passes=1, coarsen_to=0):
         """k-way partition of a host Graph (cm_part_graph).  Returns
         (part, edge_cut, stats dict)."""
         from . import cm_part_params, cm_part_stats, _np_p

@@ -4,10 +4,11 @@ import ctypes
 
 import numpy as np
 
-from . import (Graph, cm_batch_stats, cm_graph, cm_job_info, cm_part_params, lib, _check, _np_p, MATCH_HEM)
+from . import (Graph, cm_batch_stats, cm_graph, cm_job_info, cm_part_params, lib, _check, _np_p,
+               MATCH_HEM_HASH)
 
 
-def _params(seed=1, mode=MATCH_HEM, refine_passes=1, coarsen_to=0):
+def _params(seed=1, mode=MATCH_HEM_HASH, refine_passes=1, coarsen_to=0):
     return cm_part_params(int(seed), int(mode), int(refine_passes), int(coarsen_to))
 
 
@@ -27,7 +28,7 @@ class Engine:
                                       int(reserve_nvtxs), int(reserve_nedges), ctypes.byref(h)))
         self._h = h
 
-    def submit(self, g, nparts, seed=1, mode=MATCH_HEM, refine_passes=1, coarsen_to=0):
+    def submit(self, g, nparts, seed=1, mode=MATCH_HEM_HASH, refine_passes=1, coarsen_to=0):
         part = np.zeros(max(g.nvtxs, 1), np.int32)
         jid = ctypes.c_int64(0)
         cg = g.as_cm()
@@ -66,7 +67,7 @@ class Engine:
         self.close()
 
 
-def part_batch(graphs, nparts, device=0, workers=8, seed=1, mode=MATCH_HEM):
+def part_batch(graphs, nparts, device=0, workers=8, seed=1, mode=MATCH_HEM_HASH):
     """Partitions a list of host Graphs (cm_part_batch).  nparts: int or one
     per graph.  Returns (list of parts, edge cuts, stats dict)."""
     nb = len(graphs)

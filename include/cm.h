@@ -259,7 +259,7 @@ int cm_project(cm_ctx *ctx, int32_t n, const int32_t *d_cmap, const int32_t *d_c
 
 typedef struct cm_part_params {
   int32_t seed;          /* initial-partition rand() seed (1 = the reference's stream) */
-  int32_t match_mode;    /* CM_MATCH_* for the coarsening                          */
+  int32_t match_mode;    /* CM_MATCH_* for the coarsening (default CM_MATCH_HEM_HASH) */
   int32_t refine_passes; /* refinement passes per level (the reference: 1)        */
   int32_t coarsen_to;    /* 0: max(n / (20 log2 k), 30 k) (cuMetis.cu:3634)         */
 } cm_part_params;

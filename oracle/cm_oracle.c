@@ -362,3 +362,70 @@ int64_t or_ref_cpu_contract(int32_t n, const int32_t *xadj, const int32_t *adjnc
   free(htable);
   return cne;
 }
+
+/* ---------------------------------------------------------------------- */
+/* One k-way refinement pass of the reference (cu:3236-3514), with the part */
+/* groups run one after another in part order (the reference runs them as  */
+/* concurrent threads).  Boundary: weight to other parts > weight to own;   */
+/* target: first part id of largest connection if it beats the own part;    */
+/* groups by target in vertex order; phase 1 moves to higher part ids,      */
+/* phase 2 to lower, each only if both parts stay in their windows.         */
+/* Returns the number of moves.                                             */
+/* ---------------------------------------------------------------------- */
+int64_t or_refine_kway(int32_t n, const int32_t *xadj, const int32_t *adjncy, const int32_t *adjwgt,
+                       const int32_t *vwgt, int32_t k, int32_t *where) {
+  int64_t tv = 0;
+  for (int32_t v = 0; v < n; ++v) tv += vwgt[v];
+  const float tp = (float)(1.0 / k);
+  const float x = tp * (float)(int32_t)tv;
+  const int32_t mx = (int32_t)(x * 1.03f), mn = (int32_t)(x / 1.03f);
+  int64_t *pw = (int64_t *)calloc((size_t)k, sizeof(int64_t));
+  int64_t *acc = (int64_t *)calloc((size_t)k, sizeof(int64_t));
+  int32_t *target = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n ? n : 1));
+  int32_t *flag = (int32_t *)calloc((size_t)(n ? n : 1), sizeof(int32_t));
+  int32_t *cnt = (int32_t *)calloc((size_t)k + 1, sizeof(int32_t));
+  int32_t *order = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n ? n : 1));
+  for (int32_t v = 0; v < n; ++v) pw[where[v]] += vwgt[v];
+  for (int32_t v = 0; v < n; ++v) {
+    const int32_t me = where[v];
+    int64_t mw = 0, ow = 0;
+    for (int32_t j = xadj[v]; j < xadj[v + 1]; ++j) {
+      if (where[adjncy[j]] == me) mw += adjwgt[j];
+      else ow += adjwgt[j];
+    }
+    target[v] = me;
+    if (ow > mw) {
+      flag[v] = 1;
+      for (int32_t j = xadj[v]; j < xadj[v + 1]; ++j) acc[where[adjncy[j]]] += adjwgt[j];
+      int64_t best = acc[me];
+      int32_t bp = me;
+      for (int32_t j = xadj[v]; j < xadj[v + 1]; ++j) {
+        const int32_t p = where[adjncy[j]];
+        if (acc[p] > best || (acc[p] == best && bp != me && p < bp)) { best = acc[p]; bp = p; }
+      }
+      target[v] = bp;
+      cnt[bp + 1]++;
+      for (int32_t j = xadj[v]; j < xadj[v + 1]; ++j) acc[where[adjncy[j]]] = 0;
+    }
+  }
+  for (int32_t t = 0; t < k; ++t) cnt[t + 1] += cnt[t];
+  for (int32_t v = 0; v < n; ++v)
+    if (flag[v]) order[cnt[target[v]]++] = v;   /* stable: vertex order within a group */
+  for (int32_t t = k; t > 0; --t) cnt[t] = cnt[t - 1];
+  cnt[0] = 0;
+  int64_t moves = 0;
+  for (int phase = 0; phase < 2; ++phase)
+    for (int32_t t = 0; t < k; ++t)
+      for (int32_t i = cnt[t]; i < cnt[t + 1]; ++i) {
+        const int32_t v = order[i], me = where[v], w = vwgt[v];
+        if (phase == 0 ? me >= t : me <= t) continue;
+        if (pw[t] + w >= mn && pw[t] + w <= mx && pw[me] - w >= mn && pw[me] - w <= mx) {
+          pw[t] += w;
+          pw[me] -= w;
+          where[v] = t;
+          ++moves;
+        }
+      }
+  free(pw); free(acc); free(target); free(flag); free(cnt); free(order);
+  return moves;
+}

@@ -44,6 +44,8 @@ def lib():
         L.or_ref_cpu_contract.restype = ctypes.c_int64
         L.or_ref_cpu_contract.argtypes = [ctypes.c_int32, _I32P, _I32P, _I32P, _I32P, _I32P, _I32P, ctypes.c_int32,
                                           _I32P, _I32P, _I32P, _I32P]
+        L.or_refine_kway.restype = ctypes.c_int64
+        L.or_refine_kway.argtypes = [ctypes.c_int32, _I32P, _I32P, _I32P, _I32P, ctypes.c_int32, _I32P]
         L.or_edge_hash.restype = ctypes.c_uint32
         L.or_edge_hash.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
         L.srand_seed = ctypes.CDLL(None).srand
@@ -226,11 +228,12 @@ def match_from_cmap(cmap):
 def ref_harness_rbbisection(g, nparts, seed):
     """The reference's own initial partition (cuMetis_rbbisection,
     cuMetis.cu:3046) of graph g into nparts, with its rand() stream seeded by
-    srand(seed).  Returns (part, objval)."""
+    srand(seed) (seed None: the stream continues).  Returns (part, objval)."""
     R = ref()
     if R is None:
         raise RuntimeError("reference harness not built (reference tree absent)")
-    R.ref_srand(ctypes.c_uint(seed))
+    if seed is not None:
+        R.ref_srand(ctypes.c_uint(seed))
     part = np.zeros(max(g.n, 1), np.int32)
     obj = np.zeros(1, np.int32)
     R.ref_rbbisection(ctypes.c_int32(g.n), _p(g.xadj), _p(g.adjncy), _p(g.vwgt), _p(g.adjwgt),
@@ -300,3 +303,11 @@ def refine_kway_model(g, where, k):
                     where[v] = t
                     moves += 1
     return where, moves
+
+
+def refine_kway_c(g, where, k):
+    """C restatement of refine_kway_model (same rules, same group order), for
+    graphs too large for the Python loop.  Returns (where, moves)."""
+    w = np.array(where, np.int32).copy()
+    mv = lib().or_refine_kway(g.n, _p(g.xadj), _p(g.adjncy), _p(g.adjwgt), _p(g.vwgt), int(k), _p(w))
+    return w, int(mv)

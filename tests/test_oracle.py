@@ -137,3 +137,16 @@ def test_coarsen_loop_stop_rule():
     assert ns[0] == 4761 and ns[-1] <= 240 or ns[-1] >= 0.75 * ns[-2]
     for a, b in zip(ns, ns[1:]):
         assert b < a
+
+
+def test_refine_model_c_equals_python():
+    import cumetis_gb300 as cm
+    for g, k in ((cm.gen_tri_grid(40, 40), 2), (cm.gen_tri_grid(40, 40), 8), (cm.gen_rmat(10, 16, seed=3), 16),
+                 (cm.gen_grid2d(30, 50), 64)):
+        og = O.CSR(g.xadj, g.adjncy, g.adjwgt, g.vwgt)
+        rng = np.random.default_rng(k)
+        where = rng.integers(0, k, g.nvtxs).astype(np.int32)
+        a, ma = O.refine_kway_model(og, where, k)
+        b, mb = O.refine_kway_c(og, where, k)
+        np.testing.assert_array_equal(a, b)
+        assert ma == mb

@@ -102,7 +102,7 @@ def test_project(ctx):
 
 
 def _pipeline_model(g, k, seed, threshold):
-    levels = O.coarsen(_o(g), threshold)
+    levels = O.coarsen(_o(g), threshold, mode=1)  # cm_part_graph's default: hash-ordered ties
     coarsest = levels[-1][0]
     where, _ = cm.initial_partition(cm.Graph(coarsest.xadj, coarsest.adjncy, coarsest.adjwgt, coarsest.vwgt), k, seed)
     where = np.asarray(where, np.int32)
