@@ -361,7 +361,8 @@ def main():
     ap.add_argument("--hbm-budget-gb", type=float, default=200.0, help="serve: admission budget")
     ap.add_argument("--max-queue", type=int, default=64, help="serve: waiting jobs before submissions are rejected")
     ap.add_argument("--drain", type=float, default=10.0, help="serve: seconds to wait for admitted jobs")
-    ap.add_argument("--mode", type=int, default=0, help="matching mode (0 = heaviest edge, ties to lower id)")
+    ap.add_argument("--mode", type=int, default=1,
+                    help="matching tie order: 1 = edge hash (default), 0 = lower vertex id")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) measurement")
     args = ap.parse_args()

@@ -61,6 +61,7 @@ struct MatchArgs {
   Slot slot[2];
   int *nsmall, *nupd, *nact;     // [2] each
   unsigned long long *big;       // [2] = (rows << 32 | chunks)
+  int *vmax;                     // largest vertex weight (zeroed before the launch)
   int *part;                     // per chunk: kTop x (w, h, k)
   int max_rounds;
   DevStatus *st;
@@ -194,7 +195,8 @@ __device__ __forceinline__ TopK<H, KK> warp_topk(const TopK<H, KK> &t) {
 // Per-lane best KK over entries [b, e) (e - b <= kChunk) of v's row; all loads
 // of the chunk are issued before any is used.
 template <bool H, int KK>
-__device__ __forceinline__ TopK<H, KK> lane_scan(const MatchArgs &a, int v, long long vw, int b, int e) {
+__device__ __forceinline__ TopK<H, KK> lane_scan(const MatchArgs &a, int v, long long vw, int b, int e,
+                                                 bool all_elig = false) {
   const int lane = threadIdx.x & 31;
   constexpr int U = kChunk / 32;
   int k[U], w[U], s[U];
@@ -205,11 +207,12 @@ __device__ __forceinline__ TopK<H, KK> lane_scan(const MatchArgs &a, int v, long
     w[u] = j < e ? a.adjwgt[j] : 0;
   }
 #pragma unroll
-  for (int u = 0; u < U; ++u) s[u] = k[u] >= 0 ? __ldcg(a.m2 + k[u]) : 0;
+  for (int u = 0; u < U; ++u) s[u] = (k[u] >= 0 && !all_elig) ? __ldcg(a.m2 + k[u]) : -1;
   TopK<H, KK> t;
 #pragma unroll
   for (int u = 0; u < U; ++u)
-    if (k[u] >= 0 && eligible<H>(a, vw, v, k[u], s[u])) t.insert(Cand<H>::make(v, k[u], w[u]));
+    if (k[u] >= 0 && (all_elig ? k[u] != v : eligible<H>(a, vw, v, k[u], s[u])))
+      t.insert(Cand<H>::make(v, k[u], w[u]));
   return t;
 }
 
@@ -309,13 +312,23 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
     a.nsmall[0] = a.nsmall[1] = a.nupd[0] = a.nupd[1] = a.nact[0] = a.nact[1] = 0;
     a.big[0] = a.big[1] = 0;
   }
+  int wmax = 0;
   for (long long v = gthread; v < n; v += nthreads) {
-    a.m2[v] = -1 - a.vwgt[v];
+    const int vw0 = a.vwgt[v];
+    wmax = max(wmax, vw0);
+    a.m2[v] = -1 - vw0;
     a.ptr[v] = -1;
     a.stamp[v] = 0;
     a.top[v * kTop] = kNotScanned;
   }
+  wmax = __reduce_max_sync(0xffffffffu, wmax);
+  if (lane == 0 && wmax > 0) atomicMax(a.vmax, wmax);
   if (!grid_barrier(st, gridDim.x)) return;
+  // When even the two heaviest vertices may pair and are light (2 vmax <=
+  // maxvwgt, 3 vmax < maxvwgt), every edge is eligible while nothing is
+  // matched: the first round then needs no neighbour-state gathers.
+  const long long vmax = __ldcg(a.vmax);
+  const bool all_elig0 = 2 * vmax <= a.maxvwgt && 3 * vmax < a.maxvwgt;
   // Round 0 scans every vertex that has a neighbour: short rows straight from
   // the vertex range, longer rows through the chunk list built here.
   for (long long b0 = (long long)gwarp * 32; b0 < n; b0 += (long long)nwarps * 32) {
@@ -357,6 +370,7 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
     // A vertex's first scan keeps only its best candidate (most vertices never
     // need more); a rescan fills the whole cache.
     const bool first = round == 0;
+    const bool skip_gather = first && all_elig0;
 
     // ---- phase A: full scans -------------------------------------------------
     for (long long b0 = (long long)gwarp * 32; b0 < nsmall; b0 += (long long)nwarps * 32) {
@@ -365,6 +379,20 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
       const int v = first ? (int)i : __ldcg(S.small + i);
       const int xs = a.xadj[v], deg = a.xadj[v + 1] - xs;
       if (first && (deg == 0 || deg > kSerialDeg)) continue;
+      if (skip_gather) {  // first round, every edge eligible: ids and weights only
+        int k[kSerialDeg], w[kSerialDeg];
+#pragma unroll
+        for (int t = 0; t < kSerialDeg; ++t) {
+          k[t] = t < deg ? a.adjncy[xs + t] : -1;
+          w[t] = t < deg ? a.adjwgt[xs + t] : 0;
+        }
+        TopK<H, 1> tk;
+#pragma unroll
+        for (int t = 0; t < kSerialDeg; ++t)
+          if (k[t] >= 0 && k[t] != v) tk.insert(Cand<H>::make(v, k[t], w[t]));
+        store_top(a, v, tk);
+        continue;
+      }
       const int sv = __ldcg(a.m2 + v);
       if (sv >= 0) continue;
       const long long vw = -1ll - sv;
@@ -372,22 +400,56 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
 #pragma unroll
       for (int t = 0; t < kSerialDeg; ++t) k[t] = t < deg ? a.adjncy[xs + t] : -1;
 #pragma unroll
-      for (int t = 0; t < kSerialDeg; ++t) s[t] = k[t] >= 0 ? __ldcg(a.m2 + k[t]) : 0;
+      for (int t = 0; t < kSerialDeg; ++t) s[t] = (k[t] >= 0 && !skip_gather) ? __ldcg(a.m2 + k[t]) : -1;
       if (first) {
         TopK<H, 1> tk;
 #pragma unroll
         for (int t = 0; t < kSerialDeg; ++t)
-          if (k[t] >= 0 && eligible<H>(a, vw, v, k[t], s[t])) tk.insert(Cand<H>::make(v, k[t], a.adjwgt[xs + t]));
+          if (k[t] >= 0 && (skip_gather ? k[t] != v : eligible<H>(a, vw, v, k[t], s[t])))
+            tk.insert(Cand<H>::make(v, k[t], a.adjwgt[xs + t]));
         store_top(a, v, tk);
       } else {
         TopK<H, kTop> tk;
 #pragma unroll
         for (int t = 0; t < kSerialDeg; ++t)
-          if (k[t] >= 0 && eligible<H>(a, vw, v, k[t], s[t])) tk.insert(Cand<H>::make(v, k[t], a.adjwgt[xs + t]));
+          if (k[t] >= 0 && (skip_gather ? k[t] != v : eligible<H>(a, vw, v, k[t], s[t])))
+            tk.insert(Cand<H>::make(v, k[t], a.adjwgt[xs + t]));
         store_top(a, v, tk);
       }
     }
-    for (int q = gwarp; q < nchunks; q += nwarps) {
+    if (skip_gather) {
+      // First round, every edge eligible: no neighbour state, the next chunk's
+      // descriptor loaded ahead, multi-chunk rows merge one partial per chunk.
+      int4 d = gwarp < nchunks ? __ldcg(S.desc + gwarp) : make_int4(0, 0, 0, 0);
+      for (int q = gwarp; q < nchunks; q += nwarps) {
+        const int4 dn = q + nwarps < nchunks ? __ldcg(S.desc + q + nwarps) : d;
+        const int v = d.x, i = d.w;
+        const TopK<H, 1> r1 = warp_topk(lane_scan<H, 1>(a, v, 0, d.y, d.z, true));
+        if (i < 0) {
+          if (lane == 0) store_top(a, v, r1);
+        } else {
+          const int nch = (a.xadj[v + 1] - a.xadj[v] + kChunk - 1) / kChunk;
+          int last = 0;
+          if (lane == 0) {
+            r1.c[0].store(a.part + (size_t)q * kTop * kPartInts);
+            __threadfence();
+            last = atomicAdd(S.big_done + i, 1) == nch - 1;
+          }
+          last = __shfl_sync(0xffffffffu, last, 0);
+          if (last) {
+            __threadfence();
+            const int base = __ldcg(S.big_base + i);
+            TopK<H, 1> acc;
+            for (int t = lane; t < nch; t += 32)
+              acc.insert(Cand<H>::load(a.part + (size_t)(base + t) * kTop * kPartInts));
+            const TopK<H, 1> rr = warp_topk(acc);
+            if (lane == 0) store_top(a, v, rr);
+          }
+        }
+        d = dn;
+      }
+    }
+    for (int q = skip_gather ? nchunks : gwarp; q < nchunks; q += nwarps) {
       const int4 d = __ldcg(S.desc + q);
       const int v = d.x, i = d.w;
       const int sv = __ldcg(a.m2 + v);
@@ -395,7 +457,7 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
       const long long vw = -1ll - sv;
       TopK<H, kTop> r;
       if (first) {
-        const TopK<H, 1> r1 = warp_topk(lane_scan<H, 1>(a, v, vw, d.y, d.z));
+        const TopK<H, 1> r1 = warp_topk(lane_scan<H, 1>(a, v, vw, d.y, d.z, skip_gather));
         r.c[0] = r1.c[0];
       } else {
         r = warp_topk(lane_scan<H, kTop>(a, v, vw, d.y, d.z));
@@ -598,7 +660,9 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
   a.nupd = take(64);
   a.nact = take(64);
   a.big = (unsigned long long *)take(64);
+  a.vmax = take(64);
   if (!ok) return cm_fail(CM_ERR_NOMEM, "cm_match: workspace too small");
+  cudaMemsetAsync(a.vmax, 0, sizeof(int), s);
   a.max_rounds = n + 8;
   a.st = ctx->d_status;
   a.trace = ctx->d_trace;
