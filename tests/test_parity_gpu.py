@@ -271,6 +271,41 @@ def test_grid725_full_size_bitexact(ctx):
             assert np.array_equal(hm, wm)
 
 
+def test_large_ids_use_64bit_tile_keys(ctx):
+    """n above 2^23 - 1 coarse ids: the tiles switch to 64-bit (row, id)
+    keys.  A 2900 x 2900 grid (8,410,000 vertices), both tie orders for the
+    matching, contraction bit-exact against the oracle."""
+    g = cm.gen_grid2d(2900, 2900)
+    assert g.nvtxs > (1 << 23) - 1
+    og = _o(g)
+    dg = g.to_device()
+    thr = cm.coarsen_threshold(g.nvtxs, 64)
+    mv = cm.maxvwgt_rule(g.nvtxs, thr)
+    m, _ = ctx.match(dg, mv, 1)
+    want = O.match_greedy(og, mv, 1)
+    assert np.array_equal(m.cpu().numpy(), want)
+    cg, cmap = ctx.contract(dg, m)
+    wcg, wcmap = O.contract(og, want)
+    assert np.array_equal(cmap.cpu().numpy(), wcmap)
+    assert_same_graph(_o(cg.to_host()), wcg, "grid2900")
+
+
+def test_rmat22_full_size_hash_ties(ctx):
+    """The benchmark's tie order on the benchmark's graph: matching bit-exact
+    against the oracle, coarse graph bit-exact."""
+    g = cm.gen_rmat(22, 16, seed=1)
+    thr = cm.coarsen_threshold(g.nvtxs, 256)
+    mv = cm.maxvwgt_rule(g.nvtxs, thr)
+    og = _o(g)
+    dg = g.to_device()
+    m, rounds = ctx.match(dg, mv, 1)
+    want = O.match_greedy(og, mv, 1)
+    assert np.array_equal(m.cpu().numpy(), want)
+    cg, cmap = ctx.contract(dg, m)
+    wcg, _ = O.contract(og, want)
+    assert_same_graph(_o(cg.to_host()), wcg, "rmat22 hash")
+
+
 def test_rmat22_full_size(ctx):
     """R-MAT scale 22 (the throughput workload): matching bit-exact against
     the oracle; contraction checked by invariants (total vertex weight,
