@@ -56,6 +56,7 @@ def build(force=False, bounds_check=False, verbose=False):
     os.makedirs(BUILD, exist_ok=True)
     deps = _deps()
     extra = ["-DCM_BOUNDS_CHECK=1"] if bounds_check or os.environ.get("CM_BOUNDS_CHECK") == "1" else []
+    extra += os.environ.get("CM_EXTRA_DEFINES", "").split()  # e.g. "-DCM_MID_THREADS0=512" for tuning runs
     jobs, objs = [], []
     for f in CU_SOURCES:
         src = os.path.join(CSRC, f)

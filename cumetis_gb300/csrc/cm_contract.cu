@@ -45,6 +45,15 @@ constexpr int kTileCap = kTileDiag + kLongThr;    // max entries in a tile (mult
 constexpr int kHashCap = 4096;                    // count-pass hash slots (power of two >= 2 kTileCap)
 constexpr int kChunk = 8192;                      // long-row chunk (entries sorted per block)
 constexpr int kChunkThreads = 1024;
+// Threads per block of the three size classes of rows between kLongThr and
+// kChunk entries (1025-2048, 2049-4096, 4097-8192).
+#ifndef CM_MID_THREADS0
+#define CM_MID_THREADS0 256
+#endif
+#ifndef CM_MID_THREADS1
+#define CM_MID_THREADS1 512
+#endif
+constexpr int kMidThreads0 = CM_MID_THREADS0, kMidThreads1 = CM_MID_THREADS1;
 
 // Composite key (tile-local row, coarse id).  32-bit when coarse ids fit in
 // 23 bits (n < 2^23 - 1; rows need 9 bits for kTileDiag = 512), else 64-bit.
@@ -413,9 +422,9 @@ __host__ __device__ __forceinline__ int merge_passes(int L) {
 }
 
 // Chunked rows carry packed entries (coarse id << 32 | weight) through the
-// sort and merge passes.  A self loop gets the id kSelfKey: it sorts after
-// every coarse id (< 2^31) and keeps the packed word below the all-ones pad.
-constexpr unsigned kSelfKey = 0xfffffffeu;
+// merge passes.  Pad entries have the id kPadId, above every coarse id
+// (< 2^31 - 1), so they sort to the end of every merged run.
+constexpr unsigned kPadId = 0x7fffffffu;
 __device__ __forceinline__ unsigned long long pack_entry(int2 e) {
   return ((unsigned long long)(unsigned)e.x << 32) | (unsigned)e.y;
 }
@@ -423,14 +432,7 @@ __device__ __forceinline__ int2 unpack_entry(unsigned long long v) {
   return make_int2((int)(unsigned)(v >> 32), (int)(unsigned)v);
 }
 
-struct ChunkSmem {
-  unsigned long long v[2][padded_k<unsigned long long>(kChunk)];
-};
-
-// Rows too long for a tile but <= kChunk entries, one size class per launch:
-// one block merges one whole row's duplicates in a shared-memory hash set,
-// sorts the unique coarse ids and writes them with their summed weights to
-// stage[eoff[c] ...); ucount[c] = unique entries.
+// Shared memory of one block that merges and sorts up to CAP entries.
 template <int CAP>
 struct MidSmem {
   unsigned keys[2][padded_k<unsigned>(CAP + 8)];
@@ -441,6 +443,57 @@ struct MidSmem {
 
 __host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v >> 1); }
 
+// Gathers entries [cs, cs + cnt) of coarse row c's expanded row (metadata
+// md), merges duplicates in a shared-memory hash set that sums the weights
+// (self loops dropped), sorts the unique coarse ids (register runs, then
+// merge passes) and writes them with their weights to dst[0 .. U).  Returns U.
+// All NT threads call it; cnt <= CAP.
+template <int NT, int CAP>
+__device__ int unique_sorted_segment(MidSmem<CAP> &S, int c, const int4 &md, int cs, int cnt,
+                                     const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
+                                     const int *__restrict__ cmap, int2 *__restrict__ dst) {
+  constexpr int kLg = ilog2(2 * CAP);
+  const int lg = hash_log2(cnt, kLg);
+  const int hsize = 1 << lg, shift = 64 - lg;
+  const unsigned hmask = hsize - 1;
+  if (threadIdx.x == 0) S.ctr = 0;
+  for (int t = threadIdx.x; t < hsize; t += NT) {
+    S.hk[t] = ~0u;
+    S.hw[t] = 0;
+  }
+  __syncthreads();
+  for (int t0 = threadIdx.x; t0 < cnt; t0 += 4 * NT) {
+    int src[4], x[4], w[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int t = t0 + u * NT;
+      src[u] = t < cnt ? expanded_src(cs + t, md.x, md.y, md.z) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      x[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
+      w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (src[u] >= 0 && x[u] != c) hash_add<unsigned>(S.hk, S.hw, hmask, shift, (unsigned)x[u], w[u]);
+  }
+  __syncthreads();
+  const int U = hash_compact<unsigned, NT>(S.hk, hsize, S.keys[0], &S.ctr);
+  const int b = block_sort_keys<unsigned, NT, 8>(S.keys[0], S.keys[1], U);
+  const unsigned *sk = S.keys[b];
+  for (int t = threadIdx.x; t < U; t += NT) {
+    const unsigned k = sk[padk<unsigned>(t)];
+    dst[t] = make_int2((int)k, hash_get<unsigned>(S.hk, S.hw, hmask, shift, k));
+  }
+  return U;
+}
+
+// Rows too long for a tile but <= kChunk entries, one size class per launch:
+// one block per row writes the row's unique entries to stage[eoff[c] ...) and
+// their number to ucount[c].
 template <int NT, int CAP>
 __global__ void __launch_bounds__(NT)
 k_mid_rows(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
@@ -448,63 +501,28 @@ k_mid_rows(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const
            const int *__restrict__ count, int2 *__restrict__ stage, int *__restrict__ ucount) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MidSmem<CAP> &S = *reinterpret_cast<MidSmem<CAP> *>(smem_raw);
-  constexpr int kLg = ilog2(2 * CAP);
   const int nrows = *count;
   for (int i = blockIdx.x; i < nrows; i += gridDim.x) {
     const int c = list[i];
     const int4 md = row_meta[c];
-    const int L = min(md.w, CAP);
-    const int lg = hash_log2(L, kLg);
-    const int hsize = 1 << lg, shift = 64 - lg;
-    const unsigned hmask = hsize - 1;
-    if (threadIdx.x == 0) S.ctr = 0;
-    for (int t = threadIdx.x; t < hsize; t += NT) {
-      S.hk[t] = ~0u;
-      S.hw[t] = 0;
-    }
-    __syncthreads();
-    for (int t0 = threadIdx.x; t0 < L; t0 += 4 * NT) {
-      int src[4], x[4], w[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int t = t0 + u * NT;
-        src[u] = t < L ? expanded_src(t, md.x, md.y, md.z) : -1;
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        x[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
-        w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : 0;
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-        if (src[u] >= 0 && x[u] != c) hash_add<unsigned>(S.hk, S.hw, hmask, shift, (unsigned)x[u], w[u]);
-    }
-    __syncthreads();
-    const int U = hash_compact<unsigned, NT>(S.hk, hsize, S.keys[0], &S.ctr);
-    const int b = block_sort_keys<unsigned, NT, 8>(S.keys[0], S.keys[1], U);
-    const unsigned *sk = S.keys[b];
-    int2 *dst = stage + eoff[c];
-    for (int t = threadIdx.x; t < U; t += NT) {
-      const unsigned k = sk[padk<unsigned>(t)];
-      dst[t] = make_int2((int)k, hash_get<unsigned>(S.hk, S.hw, hmask, shift, k));
-    }
+    const int U = unique_sorted_segment<NT, CAP>(S, c, md, 0, min(md.w, CAP), adjncy, adjwgt, cmap, stage + eoff[c]);
     if (threadIdx.x == 0) ucount[c] = U;
     __syncthreads();
   }
 }
 
-// Rows longer than kChunk: each chunk of kChunk entries is gathered, sorted
-// in shared memory (register runs of 8, then merge passes) and written to
-// stage0 as one run for the merge passes.
+// Rows longer than kChunk: each chunk of kChunk entries becomes one sorted run
+// in stage0 for the merge passes -- its unique entries (duplicates within the
+// chunk already merged, self loops dropped), then pad entries up to the
+// chunk's length, which sort after every coarse id and are skipped by the
+// dedup.
 __global__ void __launch_bounds__(kChunkThreads, 1)
 k_long_sort(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
             const int *__restrict__ eoff, const int4 *__restrict__ row_meta, const int *__restrict__ long_list,
             const int *__restrict__ chunk_row, const unsigned long long *long_ctr, int2 *__restrict__ stage,
             int *__restrict__ ucount) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  ChunkSmem &S = *reinterpret_cast<ChunkSmem *>(smem_raw);
+  MidSmem<kChunk> &S = *reinterpret_cast<MidSmem<kChunk> *>(smem_raw);
   const int nchunks = (int)(*long_ctr & 0xffffffffu);
   for (int q = blockIdx.x; q < nchunks; q += gridDim.x) {
     const int idx = chunk_row[q];
@@ -514,30 +532,9 @@ k_long_sort(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, cons
     const int cs = j * kChunk;
     const int cnt = min(kChunk, md.w - cs);
     if (j == 0 && threadIdx.x == 0) ucount[c] = 0;  // the dedup adds the chunks' counts
-    for (int t0 = threadIdx.x; t0 < cnt; t0 += 4 * kChunkThreads) {
-      int src[4], x[4], w[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int t = t0 + u * kChunkThreads;
-        src[u] = t < cnt ? expanded_src(cs + t, md.x, md.y, md.z) : -1;
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        x[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
-        w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
-      }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : 0;
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int t = t0 + u * kChunkThreads;
-        if (t < cnt) S.v[0][padk<unsigned long long>(t)] = pack_entry(make_int2(x[u] == c ? (int)kSelfKey : x[u], w[u]));
-      }
-    }
-    __syncthreads();
-    const int b = block_merge_sort_packed<kChunkThreads, 8>(S.v[0], S.v[1], cnt);
     int2 *dst = stage + eoff[c] + cs;
-    for (int t = threadIdx.x; t < cnt; t += kChunkThreads) dst[t] = unpack_entry(S.v[b][padk<unsigned long long>(t)]);
+    const int U = unique_sorted_segment<kChunkThreads, kChunk>(S, c, md, cs, cnt, adjncy, adjwgt, cmap, dst);
+    for (int t = U + threadIdx.x; t < cnt; t += kChunkThreads) dst[t] = make_int2((int)kPadId, 0);
     __syncthreads();
   }
 }
@@ -641,7 +638,7 @@ k_long_merge(int p, const int *__restrict__ long_list, const int *__restrict__ c
 
 // Merges duplicates of the chunked rows, one block per chunk of the sorted row
 // (in stage[merge_passes(L) & 1]): a head is the first entry of a run of equal
-// ids that is not a self loop; each head's run (which may reach into the next
+// ids that is not a pad; each head's run (which may reach into the next
 // chunk) is summed and written, compacted within the chunk, to the other stage
 // at eoff[c] + j*kChunk.  chunk_cnt[q] = the chunk's unique entries, also added
 // to ucount[c].
@@ -668,7 +665,7 @@ k_long_dedup(const int *__restrict__ long_list, const int *__restrict__ chunk_ro
       int2 e = make_int2(0, 0);
       if (i < hi) {
         e = src[i];
-        h = ((unsigned)e.x != kSelfKey) && (i == 0 || src[i - 1].x != e.x);
+        h = ((unsigned)e.x < kPadId) && (i == 0 || src[i - 1].x != e.x);
       }
       int tot;
       const int ex = block_exclusive_scan<kDedupThreads>(h, scan, &tot);
@@ -804,13 +801,13 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   else
     cudaFuncSetAttribute(k_contract_tiles<unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)tile_smem);
-  cudaFuncSetAttribute(k_mid_rows<256, 2 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_mid_rows<kMidThreads0, 2 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(MidSmem<2 * kLongThr>));
-  cudaFuncSetAttribute(k_mid_rows<512, 4 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(k_mid_rows<kMidThreads1, 4 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(MidSmem<4 * kLongThr>));
   cudaFuncSetAttribute(k_mid_rows<1024, kChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)sizeof(MidSmem<kChunk>));
-  cudaFuncSetAttribute(k_long_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(ChunkSmem));
+  cudaFuncSetAttribute(k_long_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MidSmem<kChunk>));
   cudaFuncSetAttribute(k_long_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MergeSmem));
 
   // Long rows on the auxiliary streams (three size classes; the chunked
@@ -821,16 +818,16 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   stage_begin(ctx, s);
   cudaEventRecord(ctx->fork_ev, s);
   for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(ctx->aux[i], ctx->fork_ev, 0);
-  k_mid_rows<256, 2 * kLongThr><<<grid_for(sms * 4, m / (kLongThr + 1)), 256, sizeof(MidSmem<2 * kLongThr>), ctx->aux[0]>>>(
+  k_mid_rows<kMidThreads0, 2 * kLongThr><<<grid_for(sms * 4, m / (kLongThr + 1)), kMidThreads0, sizeof(MidSmem<2 * kLongThr>), ctx->aux[0]>>>(
       fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list, mid_ctr + 0, stage1, ucount);
-  k_mid_rows<512, 4 * kLongThr><<<grid_for(sms * 2, m / (2 * kLongThr + 1)), 512, sizeof(MidSmem<4 * kLongThr>), ctx->aux[1]>>>(
+  k_mid_rows<kMidThreads1, 4 * kLongThr><<<grid_for(sms * 2, m / (2 * kLongThr + 1)), kMidThreads1, sizeof(MidSmem<4 * kLongThr>), ctx->aux[1]>>>(
       fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + mid_cap, mid_ctr + 1, stage1, ucount);
   k_mid_rows<1024, kChunk><<<grid_for(sms, m / (4 * kLongThr + 1)), 1024, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
       fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + 2 * mid_cap, mid_ctr + 2, stage1, ucount);
   // Grids of the chunked-row kernels scale with the most chunks the graph can
   // have (m / kChunk), so small graphs do not claim every SM.
   const int long_grid = (int)std::min<int64_t>(sms, m / kChunk / 4 + 1);
-  k_long_sort<<<long_grid, kChunkThreads, sizeof(ChunkSmem), ctx->aux[2]>>>(
+  k_long_sort<<<long_grid, kChunkThreads, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
       fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, long_list, chunk_row, ctr, stage0, ucount);
   ctx->launches += 4;
   {

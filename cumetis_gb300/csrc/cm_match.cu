@@ -43,6 +43,16 @@ constexpr int kChunk = 256;      // entries per warp work item
 constexpr int kTop = 4;          // cached candidates per vertex
 constexpr int kNotScanned = -2;  // top[v*kTop] before the first scan
 constexpr int kUnknown = -3;     // cache slot not computed (the first scan keeps only the best)
+// Candidates the first-round scans keep when every edge is eligible: short
+// rows (one lane each) and chunked rows.  1 keeps only the best (later
+// rescans fill the cache); kTop fills the cache at once.
+#ifndef CM_FIRST_KEEP_SHORT
+#define CM_FIRST_KEEP_SHORT 2
+#endif
+#ifndef CM_FIRST_KEEP_CHUNK
+#define CM_FIRST_KEEP_CHUNK 2
+#endif
+constexpr int kFirstKeepShort = CM_FIRST_KEEP_SHORT, kFirstKeepChunk = CM_FIRST_KEEP_CHUNK;
 
 struct Slot {      // lists feeding one round (double-buffered by round parity)
   int *small;      // full scans, rows <= kSerialDeg
@@ -386,7 +396,7 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
           k[t] = t < deg ? a.adjncy[xs + t] : -1;
           w[t] = t < deg ? a.adjwgt[xs + t] : 0;
         }
-        TopK<H, 1> tk;
+        TopK<H, kFirstKeepShort> tk;
 #pragma unroll
         for (int t = 0; t < kSerialDeg; ++t)
           if (k[t] >= 0 && k[t] != v) tk.insert(Cand<H>::make(v, k[t], w[t]));
@@ -424,14 +434,21 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
       for (int q = gwarp; q < nchunks; q += nwarps) {
         const int4 dn = q + nwarps < nchunks ? __ldcg(S.desc + q + nwarps) : d;
         const int v = d.x, i = d.w;
-        const TopK<H, 1> r1 = warp_topk(lane_scan<H, 1>(a, v, 0, d.y, d.z, true));
+        constexpr int KC = kFirstKeepChunk;
+        const TopK<H, KC> r1 = warp_topk(lane_scan<H, KC>(a, v, 0, d.y, d.z, true));
         if (i < 0) {
           if (lane == 0) store_top(a, v, r1);
         } else {
           const int nch = (a.xadj[v + 1] - a.xadj[v] + kChunk - 1) / kChunk;
           int last = 0;
+          if (lane < KC) {
+            Cand<H> mine = r1.c[0];
+#pragma unroll
+            for (int t = 1; t < KC; ++t)
+              if (lane == t) mine = r1.c[t];
+            mine.store(a.part + ((size_t)q * kTop + lane) * kPartInts);
+          }
           if (lane == 0) {
-            r1.c[0].store(a.part + (size_t)q * kTop * kPartInts);
             __threadfence();
             last = atomicAdd(S.big_done + i, 1) == nch - 1;
           }
@@ -439,10 +456,10 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
           if (last) {
             __threadfence();
             const int base = __ldcg(S.big_base + i);
-            TopK<H, 1> acc;
-            for (int t = lane; t < nch; t += 32)
-              acc.insert(Cand<H>::load(a.part + (size_t)(base + t) * kTop * kPartInts));
-            const TopK<H, 1> rr = warp_topk(acc);
+            TopK<H, KC> acc;
+            for (int t = lane; t < nch * KC; t += 32)
+              acc.insert(Cand<H>::load(a.part + ((size_t)(base + t / KC) * kTop + t % KC) * kPartInts));
+            const TopK<H, KC> rr = warp_topk(acc);
             if (lane == 0) store_top(a, v, rr);
           }
         }
