@@ -37,12 +37,14 @@
 namespace cm {
 namespace {
 
-constexpr int kTileThreads = 128;
+#ifndef CM_TILE_THREADS
+#define CM_TILE_THREADS 256
+#endif
+constexpr int kTileThreads = CM_TILE_THREADS;     // threads per contraction tile
 constexpr int kTileE = 4;
 constexpr int kTileDiag = 512;                    // D
 constexpr int kLongThr = 1024;                    // rows longer than this take the long path
 constexpr int kTileCap = kTileDiag + kLongThr;    // max entries in a tile (multiple of kTileE)
-constexpr int kHashCap = 4096;                    // count-pass hash slots (power of two >= 2 kTileCap)
 constexpr int kChunk = 8192;                      // long-row chunk (entries sorted per block)
 constexpr int kChunkThreads = 1024;
 // Threads per block of the three size classes of rows between kLongThr and
@@ -74,7 +76,6 @@ template <> struct KeyT<unsigned long long> {
   static __device__ __forceinline__ unsigned id(unsigned long long k) { return (unsigned)k; }
 };
 constexpr int kSmallIdLimit = (1 << 23) - 1;   // n below this uses 32-bit keys
-static_assert(kHashCap >= 2 * kTileCap && (kHashCap & (kHashCap - 1)) == 0, "count hash: power of two >= 2 cap");
 static_assert(kTileDiag <= 512, "tile rows must fit in 9 bits");
 
 __device__ __forceinline__ int upper_bound_smem(const int *a, int n, int x) {
@@ -363,11 +364,12 @@ k_count_scan(const int *__restrict__ ucount, const int *d_cn, int *__restrict__ 
 
 // Copies the short rows' unique entries from the stage to their final place
 // cxadj[c] (one block per tile, one thread per entry).
-__global__ void __launch_bounds__(kTileThreads)
+constexpr int kCopyThreads = 128;
+__global__ void __launch_bounds__(kCopyThreads)
 k_copy_tiles(const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
              const int *__restrict__ ucount, const int *__restrict__ cxadj, const int2 *__restrict__ stage,
              int *__restrict__ cadjncy, int *__restrict__ cadjwgt) {
-  __shared__ int s_pre[kTileDiag + 1], s_src[kTileDiag], s_dst[kTileDiag], s_scan[kTileThreads / 32 + 1];
+  __shared__ int s_pre[kTileDiag + 1], s_src[kTileDiag], s_dst[kTileDiag], s_scan[kCopyThreads / 32 + 1];
   const int tid = threadIdx.x;
   const int nc = *d_cn;
   const long long dend = (long long)nc + eoff[nc];
@@ -376,7 +378,7 @@ k_copy_tiles(const int *__restrict__ eoff, const int *d_cn, const int *__restric
   const int clo = tile <= last ? first_row[tile] : nc;
   const int chi = tile + 1 <= last ? first_row[tile + 1] : nc;
   const int R = max(0, min(kTileDiag, chi - clo));
-  constexpr int kRowsPerThread = kTileDiag / kTileThreads;
+  constexpr int kRowsPerThread = kTileDiag / kCopyThreads;
   int cnt[kRowsPerThread];
   int mysum = 0;
 #pragma unroll
@@ -393,7 +395,7 @@ k_copy_tiles(const int *__restrict__ eoff, const int *d_cn, const int *__restric
     mysum += cnt[i];
   }
   int U;
-  int ex = block_exclusive_scan<kTileThreads>(mysum, s_scan, &U);
+  int ex = block_exclusive_scan<kCopyThreads>(mysum, s_scan, &U);
 #pragma unroll
   for (int i = 0; i < kRowsPerThread; ++i) {
     const int r = tid * kRowsPerThread + i;
@@ -401,7 +403,7 @@ k_copy_tiles(const int *__restrict__ eoff, const int *d_cn, const int *__restric
     ex += cnt[i];
   }
   __syncthreads();
-  for (int o = tid; o < U; o += kTileThreads) {
+  for (int o = tid; o < U; o += kCopyThreads) {
     const int r = upper_bound_smem(s_pre, R, o) - 1;
     const int k = o - s_pre[r];
     const int2 e = stage[s_src[r] + k];
@@ -871,7 +873,7 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
                                                  stage0, stage1, chunk_cnt, ucount, coarse->xadj, coarse->adjncy,
                                                  coarse->adjwgt);
   cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
-  k_copy_tiles<<<(unsigned)ntiles, kTileThreads, 0, s>>>(eoff, d_sizes, first_row, ucount, coarse->xadj, stage1,
+  k_copy_tiles<<<(unsigned)ntiles, kCopyThreads, 0, s>>>(eoff, d_sizes, first_row, ucount, coarse->xadj, stage1,
                                                          coarse->adjncy, coarse->adjwgt);
   ctx->launches += 2;
   cudaStreamWaitEvent(s, ctx->join_ev[0], 0);
