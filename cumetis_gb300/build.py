@@ -1,7 +1,7 @@
 """Build recipe for libcm.so (CUDA kernels for sm_103a + C++ host code) and
 the `cuMetis` command-line tool, in-tree under cumetis_gb300/.
 
-    python -m cumetis_gb300.build [-f] [--debug-bounds]
+    python -m cumetis_gb300.build [-f] [-v]
 
 Translation units compile in parallel; objects go to cumetis_gb300/_build/.
 """
@@ -51,11 +51,11 @@ def _compile(args):
     return r.stdout
 
 
-def build(force=False, bounds_check=False, verbose=False):
+def build(force=False, verbose=False):
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
     deps = _deps()
-    extra = ["-DCM_BOUNDS_CHECK=1"] if bounds_check or os.environ.get("CM_BOUNDS_CHECK") == "1" else []
+    extra = []
     extra += os.environ.get("CM_EXTRA_DEFINES", "").split()  # e.g. "-DCM_MID_THREADS0=512" for tuning runs
     jobs, objs = [], []
     for f in CU_SOURCES:
@@ -92,4 +92,4 @@ def build(force=False, bounds_check=False, verbose=False):
 
 
 if __name__ == "__main__":
-    print(build(force="-f" in sys.argv, bounds_check="--debug-bounds" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="-f" in sys.argv, verbose="-v" in sys.argv))

@@ -100,15 +100,6 @@ __device__ __forceinline__ bool grid_barrier(DevStatus *st, unsigned nblocks) {
   return s_ok != 0;
 }
 
-__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
-    v = w > v ? w : v;
-  }
-  return v;
-}
-
 // Edge priority hash for the hashed tie-break (lo < hi); equals
 // or_edge_hash() of the oracle.
 __host__ __device__ __forceinline__ uint32_t edge_hash(uint32_t lo, uint32_t hi) {
@@ -224,16 +215,5 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *sh, int *total) 
   __syncthreads();
   return r;
 }
-
-#ifdef CM_BOUNDS_CHECK
-#define CM_CHECK_INDEX(st, idx, lim)                                       \
-  do {                                                                     \
-    if ((long long)(idx) < 0 || (long long)(idx) >= (long long)(lim)) {    \
-      cm::record_error((st), CM_ERR_INVALID, cm::ERR_SITE_BOUNDS);         \
-    }                                                                      \
-  } while (0)
-#else
-#define CM_CHECK_INDEX(st, idx, lim) do { } while (0)
-#endif
 
 }  // namespace cm
