@@ -173,6 +173,15 @@ struct TopK {
       if (cur.better(c[i])) { Cand<H> t = c[i]; c[i] = cur; cur = t; }
     }
   }
+  // Edge (v, k) of weight w.  In hash mode the edge hash is computed only when
+  // the weight can still enter the list (a lighter edge loses to the last
+  // entry whatever its hash); the result is that of insert(make(v, k, w)).
+  __device__ __forceinline__ void insert_edge(int v, int k, int w) {
+    if constexpr (H) {
+      if (c[KK - 1].valid() && w < c[KK - 1].w) return;
+    }
+    insert(Cand<H>::make(v, k, w));
+  }
 };
 
 template <bool H>
@@ -222,7 +231,7 @@ __device__ __forceinline__ TopK<H, KK> lane_scan(const MatchArgs &a, int v, long
 #pragma unroll
   for (int u = 0; u < U; ++u)
     if (k[u] >= 0 && (all_elig ? k[u] != v : eligible<H>(a, vw, v, k[u], s[u])))
-      t.insert(Cand<H>::make(v, k[u], w[u]));
+      t.insert_edge(v, k[u], w[u]);
   return t;
 }
 
@@ -399,7 +408,7 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
         TopK<H, kFirstKeepShort> tk;
 #pragma unroll
         for (int t = 0; t < kSerialDeg; ++t)
-          if (k[t] >= 0 && k[t] != v) tk.insert(Cand<H>::make(v, k[t], w[t]));
+          if (k[t] >= 0 && k[t] != v) tk.insert_edge(v, k[t], w[t]);
         store_top(a, v, tk);
         continue;
       }
@@ -416,14 +425,14 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
 #pragma unroll
         for (int t = 0; t < kSerialDeg; ++t)
           if (k[t] >= 0 && (skip_gather ? k[t] != v : eligible<H>(a, vw, v, k[t], s[t])))
-            tk.insert(Cand<H>::make(v, k[t], a.adjwgt[xs + t]));
+            tk.insert_edge(v, k[t], a.adjwgt[xs + t]);
         store_top(a, v, tk);
       } else {
         TopK<H, kTop> tk;
 #pragma unroll
         for (int t = 0; t < kSerialDeg; ++t)
           if (k[t] >= 0 && (skip_gather ? k[t] != v : eligible<H>(a, vw, v, k[t], s[t])))
-            tk.insert(Cand<H>::make(v, k[t], a.adjwgt[xs + t]));
+            tk.insert_edge(v, k[t], a.adjwgt[xs + t]);
         store_top(a, v, tk);
       }
     }
