@@ -36,7 +36,15 @@
 namespace cm {
 namespace {
 
-constexpr int kMatchThreads = 1024;
+// Threads per block of the persistent round kernel and the blocks per SM it
+// is compiled for (its grid is every resident block, up to the graph's need).
+#ifndef CM_MATCH_THREADS
+#define CM_MATCH_THREADS 1024
+#endif
+#ifndef CM_MATCH_MINBLOCKS
+#define CM_MATCH_MINBLOCKS 1
+#endif
+constexpr int kMatchThreads = CM_MATCH_THREADS, kMatchMinBlocks = CM_MATCH_MINBLOCKS;
 constexpr int64_t kWorkPerBlock = 32768;  // vertices + entries per block of the matching grid
 constexpr int kSerialDeg = 16;   // rows scanned by one lane
 constexpr int kChunk = 256;      // entries per warp work item
@@ -310,8 +318,208 @@ __device__ __forceinline__ void block_append(int *list, int *counter, const bool
   __syncthreads();
 }
 
+// Phase A of a round: full scans of the rows whose candidates must be
+// recomputed -- rows of <= kSerialDeg entries one lane each (the whole vertex
+// range in the first round), longer rows as kChunk-entry warp chunks with a
+// last-chunk merge.  `first`: the first round (keeps kFirstKeep* candidates);
+// `skip_gather`: first round with every edge eligible (no neighbour state).
 template <bool H>
-__global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
+__device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool first, bool skip_gather,
+                                        long long nsmall, int nchunks, int gwarp, int nwarps, int lane) {
+  for (long long b0 = (long long)gwarp * 32; b0 < nsmall; b0 += (long long)nwarps * 32) {
+    const long long i = b0 + lane;
+    if (i >= nsmall) continue;
+    const int v = first ? (int)i : __ldcg(S.small + i);
+    const int xs = a.xadj[v], deg = a.xadj[v + 1] - xs;
+    if (first && (deg == 0 || deg > kSerialDeg)) continue;
+    if (skip_gather) {  // first round, every edge eligible: ids and weights only
+      int k[kSerialDeg], w[kSerialDeg];
+#pragma unroll
+      for (int t = 0; t < kSerialDeg; ++t) {
+        k[t] = t < deg ? a.adjncy[xs + t] : -1;
+        w[t] = t < deg ? a.adjwgt[xs + t] : 0;
+      }
+      TopK<H, kFirstKeepShort> tk;
+#pragma unroll
+      for (int t = 0; t < kSerialDeg; ++t)
+        if (k[t] >= 0 && k[t] != v) tk.insert_edge(v, k[t], w[t]);
+      store_top(a, v, tk);
+      continue;
+    }
+    const int sv = __ldcg(a.m2 + v);
+    if (sv >= 0) continue;
+    const long long vw = -1ll - sv;
+    int k[kSerialDeg], s[kSerialDeg];
+#pragma unroll
+    for (int t = 0; t < kSerialDeg; ++t) k[t] = t < deg ? a.adjncy[xs + t] : -1;
+#pragma unroll
+    for (int t = 0; t < kSerialDeg; ++t) s[t] = (k[t] >= 0 && !skip_gather) ? __ldcg(a.m2 + k[t]) : -1;
+    if (first) {
+      TopK<H, 1> tk;
+#pragma unroll
+      for (int t = 0; t < kSerialDeg; ++t)
+        if (k[t] >= 0 && (skip_gather ? k[t] != v : eligible<H>(a, vw, v, k[t], s[t])))
+          tk.insert_edge(v, k[t], a.adjwgt[xs + t]);
+      store_top(a, v, tk);
+    } else {
+      TopK<H, kTop> tk;
+#pragma unroll
+      for (int t = 0; t < kSerialDeg; ++t)
+        if (k[t] >= 0 && (skip_gather ? k[t] != v : eligible<H>(a, vw, v, k[t], s[t])))
+          tk.insert_edge(v, k[t], a.adjwgt[xs + t]);
+      store_top(a, v, tk);
+    }
+  }
+  if (skip_gather) {
+    // First round, every edge eligible: no neighbour state, the next chunk's
+    // descriptor loaded ahead, multi-chunk rows merge one partial per chunk.
+    int4 d = gwarp < nchunks ? __ldcg(S.desc + gwarp) : make_int4(0, 0, 0, 0);
+    for (int q = gwarp; q < nchunks; q += nwarps) {
+      const int4 dn = q + nwarps < nchunks ? __ldcg(S.desc + q + nwarps) : d;
+      const int v = d.x, i = d.w;
+      constexpr int KC = kFirstKeepChunk;
+      const TopK<H, KC> r1 = warp_topk(lane_scan<H, KC>(a, v, 0, d.y, d.z, true));
+      if (i < 0) {
+        if (lane == 0) store_top(a, v, r1);
+      } else {
+        const int nch = (a.xadj[v + 1] - a.xadj[v] + kChunk - 1) / kChunk;
+        int last = 0;
+        if (lane < KC) {
+          Cand<H> mine = r1.c[0];
+#pragma unroll
+          for (int t = 1; t < KC; ++t)
+            if (lane == t) mine = r1.c[t];
+          mine.store(a.part + ((size_t)q * kTop + lane) * kPartInts);
+        }
+        if (lane == 0) {
+          __threadfence();
+          last = atomicAdd(S.big_done + i, 1) == nch - 1;
+        }
+        last = __shfl_sync(0xffffffffu, last, 0);
+        if (last) {
+          __threadfence();
+          const int base = __ldcg(S.big_base + i);
+          TopK<H, KC> acc;
+          for (int t = lane; t < nch * KC; t += 32)
+            acc.insert(Cand<H>::load(a.part + ((size_t)(base + t / KC) * kTop + t % KC) * kPartInts));
+          const TopK<H, KC> rr = warp_topk(acc);
+          if (lane == 0) store_top(a, v, rr);
+        }
+      }
+      d = dn;
+    }
+  }
+  for (int q = skip_gather ? nchunks : gwarp; q < nchunks; q += nwarps) {
+    const int4 d = __ldcg(S.desc + q);
+    const int v = d.x, i = d.w;
+    const int sv = __ldcg(a.m2 + v);
+    if (sv >= 0) continue;  // uniform per warp
+    const long long vw = -1ll - sv;
+    TopK<H, kTop> r;
+    if (first) {
+      const TopK<H, 1> r1 = warp_topk(lane_scan<H, 1>(a, v, vw, d.y, d.z, skip_gather));
+      r.c[0] = r1.c[0];
+    } else {
+      r = warp_topk(lane_scan<H, kTop>(a, v, vw, d.y, d.z));
+    }
+    if (i < 0) {  // the row's only chunk
+      if (lane == 0) {
+        if (first) {
+          TopK<H, 1> r1;
+          r1.c[0] = r.c[0];
+          store_top(a, v, r1);
+        } else {
+          store_top(a, v, r);
+        }
+      }
+      continue;
+    }
+    const int nch = (a.xadj[v + 1] - a.xadj[v] + kChunk - 1) / kChunk;
+    int last = 0;
+    if (lane < kTop) {
+      Cand<H> mine = r.c[0];
+#pragma unroll
+      for (int t = 1; t < kTop; ++t)
+        if (lane == t) mine = r.c[t];
+      mine.store(a.part + ((size_t)q * kTop + lane) * kPartInts);
+    }
+    if (lane == 0) {
+      __threadfence();
+      last = atomicAdd(S.big_done + i, 1) == nch - 1;
+    }
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (last) {  // merge the row's chunk lists
+      __threadfence();
+      const int base = __ldcg(S.big_base + i);
+      TopK<H, kTop> acc;
+      for (int t = lane; t < nch * kTop; t += 32)
+        acc.insert(Cand<H>::load(a.part + ((size_t)base * kTop + t) * kPartInts));
+      const TopK<H, kTop> rr = warp_topk(acc);
+      if (lane == 0) {
+        if (first) {
+          TopK<H, 1> r1;
+          r1.c[0] = rr.c[0];
+          store_top(a, v, r1);
+        } else {
+          store_top(a, v, rr);
+        }
+      }
+    }
+  }
+}
+
+// Before the rounds: initial state of every vertex (unmatched, no
+// candidate), the largest vertex weight, and the first round's chunk list of
+// rows longer than kSerialDeg.  The list counters are zeroed by the host.
+constexpr int kPrepThreads = 256;
+// Resident blocks per SM the first-round kernel is compiled for (register cap).
+#ifndef CM_FIRST_MINBLOCKS
+#define CM_FIRST_MINBLOCKS 8
+#endif
+constexpr int kFirstMinBlocks = CM_FIRST_MINBLOCKS;
+template <bool H>
+__global__ void __launch_bounds__(kPrepThreads) k_match_prep(MatchArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+  const int n = a.n;
+  int wmax = 0;
+  for (long long b0 = (long long)gwarp * 32; b0 < n; b0 += (long long)nwarps * 32) {
+    const long long v = b0 + lane;
+    int xs = 0, deg = 0;
+    if (v < n) {
+      const int vw0 = a.vwgt[v];
+      wmax = max(wmax, vw0);
+      a.m2[v] = -1 - vw0;
+      a.ptr[v] = -1;
+      a.stamp[v] = 0;
+      a.top[v * kTop] = kNotScanned;
+      xs = a.xadj[v];
+      deg = a.xadj[v + 1] - xs;
+    }
+    append_scan(a, 0, deg > kSerialDeg, (int)v, xs, deg);
+  }
+  wmax = __reduce_max_sync(0xffffffffu, wmax);
+  if (lane == 0 && wmax > 0) atomicMax(a.vmax, wmax);
+}
+
+// Phase A of the first round, as an ordinary launch with more warps per SM
+// than the persistent kernel can hold.  When even the two heaviest vertices
+// may pair and are light (2 vmax <= maxvwgt, 3 vmax < maxvwgt), every edge is
+// eligible while nothing is matched, and the scans skip the neighbour state.
+template <bool H>
+__global__ void __launch_bounds__(kPrepThreads, kFirstMinBlocks) k_match_first(MatchArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int gwarp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+  const long long vmax = __ldcg(a.vmax);
+  const bool all_elig = 2 * vmax <= a.maxvwgt && 3 * vmax < a.maxvwgt;
+  const int nchunks = (int)(__ldcg(a.big) & 0xffffffffu);
+  phase_a<H>(a, a.slot[0], true, all_elig, a.n, nchunks, gwarp, nwarps, lane);
+}
+
+template <bool H>
+__global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchArgs a) {
   __shared__ int sh_scan[kMatchThreads / 32 + 1];
   __shared__ int sh_base;
   const int lane = threadIdx.x & 31;
@@ -326,37 +534,6 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
     if (tracer && row < a.trace_rows) a.trace[row * 8 + col] = v;
   };
   trace(0, 0, global_timer_ns());
-
-  if (gthread == 0) {
-    a.nsmall[0] = a.nsmall[1] = a.nupd[0] = a.nupd[1] = a.nact[0] = a.nact[1] = 0;
-    a.big[0] = a.big[1] = 0;
-  }
-  int wmax = 0;
-  for (long long v = gthread; v < n; v += nthreads) {
-    const int vw0 = a.vwgt[v];
-    wmax = max(wmax, vw0);
-    a.m2[v] = -1 - vw0;
-    a.ptr[v] = -1;
-    a.stamp[v] = 0;
-    a.top[v * kTop] = kNotScanned;
-  }
-  wmax = __reduce_max_sync(0xffffffffu, wmax);
-  if (lane == 0 && wmax > 0) atomicMax(a.vmax, wmax);
-  if (!grid_barrier(st, gridDim.x)) return;
-  // When even the two heaviest vertices may pair and are light (2 vmax <=
-  // maxvwgt, 3 vmax < maxvwgt), every edge is eligible while nothing is
-  // matched: the first round then needs no neighbour-state gathers.
-  const long long vmax = __ldcg(a.vmax);
-  const bool all_elig0 = 2 * vmax <= a.maxvwgt && 3 * vmax < a.maxvwgt;
-  // Round 0 scans every vertex that has a neighbour: short rows straight from
-  // the vertex range, longer rows through the chunk list built here.
-  for (long long b0 = (long long)gwarp * 32; b0 < n; b0 += (long long)nwarps * 32) {
-    const long long v = b0 + lane;
-    const int xs = v < n ? a.xadj[v] : 0;
-    const int deg = v < n ? a.xadj[v + 1] - xs : 0;
-    append_scan(a, 0, deg > kSerialDeg, (int)v, xs, deg);
-  }
-  if (!grid_barrier(st, gridDim.x)) return;
 
   int round = 0;
   for (;; ++round) {
@@ -389,149 +566,9 @@ __global__ void __launch_bounds__(kMatchThreads, 1) k_match(MatchArgs a) {
     // A vertex's first scan keeps only its best candidate (most vertices never
     // need more); a rescan fills the whole cache.
     const bool first = round == 0;
-    const bool skip_gather = first && all_elig0;
 
-    // ---- phase A: full scans -------------------------------------------------
-    for (long long b0 = (long long)gwarp * 32; b0 < nsmall; b0 += (long long)nwarps * 32) {
-      const long long i = b0 + lane;
-      if (i >= nsmall) continue;
-      const int v = first ? (int)i : __ldcg(S.small + i);
-      const int xs = a.xadj[v], deg = a.xadj[v + 1] - xs;
-      if (first && (deg == 0 || deg > kSerialDeg)) continue;
-      if (skip_gather) {  // first round, every edge eligible: ids and weights only
-        int k[kSerialDeg], w[kSerialDeg];
-#pragma unroll
-        for (int t = 0; t < kSerialDeg; ++t) {
-          k[t] = t < deg ? a.adjncy[xs + t] : -1;
-          w[t] = t < deg ? a.adjwgt[xs + t] : 0;
-        }
-        TopK<H, kFirstKeepShort> tk;
-#pragma unroll
-        for (int t = 0; t < kSerialDeg; ++t)
-          if (k[t] >= 0 && k[t] != v) tk.insert_edge(v, k[t], w[t]);
-        store_top(a, v, tk);
-        continue;
-      }
-      const int sv = __ldcg(a.m2 + v);
-      if (sv >= 0) continue;
-      const long long vw = -1ll - sv;
-      int k[kSerialDeg], s[kSerialDeg];
-#pragma unroll
-      for (int t = 0; t < kSerialDeg; ++t) k[t] = t < deg ? a.adjncy[xs + t] : -1;
-#pragma unroll
-      for (int t = 0; t < kSerialDeg; ++t) s[t] = (k[t] >= 0 && !skip_gather) ? __ldcg(a.m2 + k[t]) : -1;
-      if (first) {
-        TopK<H, 1> tk;
-#pragma unroll
-        for (int t = 0; t < kSerialDeg; ++t)
-          if (k[t] >= 0 && (skip_gather ? k[t] != v : eligible<H>(a, vw, v, k[t], s[t])))
-            tk.insert_edge(v, k[t], a.adjwgt[xs + t]);
-        store_top(a, v, tk);
-      } else {
-        TopK<H, kTop> tk;
-#pragma unroll
-        for (int t = 0; t < kSerialDeg; ++t)
-          if (k[t] >= 0 && (skip_gather ? k[t] != v : eligible<H>(a, vw, v, k[t], s[t])))
-            tk.insert_edge(v, k[t], a.adjwgt[xs + t]);
-        store_top(a, v, tk);
-      }
-    }
-    if (skip_gather) {
-      // First round, every edge eligible: no neighbour state, the next chunk's
-      // descriptor loaded ahead, multi-chunk rows merge one partial per chunk.
-      int4 d = gwarp < nchunks ? __ldcg(S.desc + gwarp) : make_int4(0, 0, 0, 0);
-      for (int q = gwarp; q < nchunks; q += nwarps) {
-        const int4 dn = q + nwarps < nchunks ? __ldcg(S.desc + q + nwarps) : d;
-        const int v = d.x, i = d.w;
-        constexpr int KC = kFirstKeepChunk;
-        const TopK<H, KC> r1 = warp_topk(lane_scan<H, KC>(a, v, 0, d.y, d.z, true));
-        if (i < 0) {
-          if (lane == 0) store_top(a, v, r1);
-        } else {
-          const int nch = (a.xadj[v + 1] - a.xadj[v] + kChunk - 1) / kChunk;
-          int last = 0;
-          if (lane < KC) {
-            Cand<H> mine = r1.c[0];
-#pragma unroll
-            for (int t = 1; t < KC; ++t)
-              if (lane == t) mine = r1.c[t];
-            mine.store(a.part + ((size_t)q * kTop + lane) * kPartInts);
-          }
-          if (lane == 0) {
-            __threadfence();
-            last = atomicAdd(S.big_done + i, 1) == nch - 1;
-          }
-          last = __shfl_sync(0xffffffffu, last, 0);
-          if (last) {
-            __threadfence();
-            const int base = __ldcg(S.big_base + i);
-            TopK<H, KC> acc;
-            for (int t = lane; t < nch * KC; t += 32)
-              acc.insert(Cand<H>::load(a.part + ((size_t)(base + t / KC) * kTop + t % KC) * kPartInts));
-            const TopK<H, KC> rr = warp_topk(acc);
-            if (lane == 0) store_top(a, v, rr);
-          }
-        }
-        d = dn;
-      }
-    }
-    for (int q = skip_gather ? nchunks : gwarp; q < nchunks; q += nwarps) {
-      const int4 d = __ldcg(S.desc + q);
-      const int v = d.x, i = d.w;
-      const int sv = __ldcg(a.m2 + v);
-      if (sv >= 0) continue;  // uniform per warp
-      const long long vw = -1ll - sv;
-      TopK<H, kTop> r;
-      if (first) {
-        const TopK<H, 1> r1 = warp_topk(lane_scan<H, 1>(a, v, vw, d.y, d.z, skip_gather));
-        r.c[0] = r1.c[0];
-      } else {
-        r = warp_topk(lane_scan<H, kTop>(a, v, vw, d.y, d.z));
-      }
-      if (i < 0) {  // the row's only chunk
-        if (lane == 0) {
-          if (first) {
-            TopK<H, 1> r1;
-            r1.c[0] = r.c[0];
-            store_top(a, v, r1);
-          } else {
-            store_top(a, v, r);
-          }
-        }
-        continue;
-      }
-      const int nch = (a.xadj[v + 1] - a.xadj[v] + kChunk - 1) / kChunk;
-      int last = 0;
-      if (lane < kTop) {
-        Cand<H> mine = r.c[0];
-#pragma unroll
-        for (int t = 1; t < kTop; ++t)
-          if (lane == t) mine = r.c[t];
-        mine.store(a.part + ((size_t)q * kTop + lane) * kPartInts);
-      }
-      if (lane == 0) {
-        __threadfence();
-        last = atomicAdd(S.big_done + i, 1) == nch - 1;
-      }
-      last = __shfl_sync(0xffffffffu, last, 0);
-      if (last) {  // merge the row's chunk lists
-        __threadfence();
-        const int base = __ldcg(S.big_base + i);
-        TopK<H, kTop> acc;
-        for (int t = lane; t < nch * kTop; t += 32)
-          acc.insert(Cand<H>::load(a.part + ((size_t)base * kTop + t) * kPartInts));
-        const TopK<H, kTop> rr = warp_topk(acc);
-        if (lane == 0) {
-          if (first) {
-            TopK<H, 1> r1;
-            r1.c[0] = rr.c[0];
-            store_top(a, v, r1);
-          } else {
-            store_top(a, v, rr);
-          }
-        }
-      }
-    }
+    // ---- phase A: full scans (the first round's ran in k_match_first) ---------
+    if (!first) phase_a<H>(a, S, false, false, nsmall, nchunks, gwarp, nwarps, lane);
     if (!grid_barrier(st, gridDim.x)) return;
     trace(round + 1, 1, global_timer_ns());
 
@@ -682,13 +719,14 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
     S.act = take((size_t)n * 4);
   }
   a.part = take((size_t)ch * 4 * kPartInts * kTop);
-  a.nsmall = take(64);
-  a.nupd = take(64);
-  a.nact = take(64);
-  a.big = (unsigned long long *)take(64);
-  a.vmax = take(64);
+  int *ctrs = take(320);  // list counters of both slots and the largest vertex weight
   if (!ok) return cm_fail(CM_ERR_NOMEM, "cm_match: workspace too small");
-  cudaMemsetAsync(a.vmax, 0, sizeof(int), s);
+  a.nsmall = ctrs;
+  a.nupd = ctrs + 16;
+  a.nact = ctrs + 32;
+  a.big = (unsigned long long *)(ctrs + 48);
+  a.vmax = ctrs + 64;
+  cudaMemsetAsync(ctrs, 0, 320, s);
   a.max_rounds = n + 8;
   a.st = ctx->d_status;
   a.trace = ctx->d_trace;
@@ -703,6 +741,16 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
   const int grid = (int)std::min<int64_t>((int64_t)ctx->num_sms * per_sm, want);
   void *args[] = {(void *)&a};
   stage_begin(ctx, s);
+  const unsigned pgrid = (unsigned)std::min<int64_t>((int64_t)ctx->num_sms * 8, n / kPrepThreads + 1);
+  const unsigned fgrid = (unsigned)std::min<int64_t>((int64_t)ctx->num_sms * 8, want * 4);
+  if (mode == CM_MATCH_HEM_HASH) {
+    k_match_prep<true><<<pgrid, kPrepThreads, 0, s>>>(a);
+    k_match_first<true><<<fgrid, kPrepThreads, 0, s>>>(a);
+  } else {
+    k_match_prep<false><<<pgrid, kPrepThreads, 0, s>>>(a);
+    k_match_first<false><<<fgrid, kPrepThreads, 0, s>>>(a);
+  }
+  ctx->launches += 2;
   cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kMatchThreads), args, 0, s);
   stage_end(ctx, CM_STAGE_MATCH, s);
   if (e != cudaSuccess) return cuda_status(e, "cm_match launch");
