@@ -127,6 +127,7 @@ def _declare(L):
                                   ctypes.POINTER(cm_part_params), ctypes.POINTER(cm_part_stats)]),
         "cuMetis_PartGraph": (c_int, [_I32P, _I32P, _I32P, _I32P, _I32P, _I32P, c_vp, c_vp, _I32P, _I32P]),
         "cm_ctx_stream": (c_vp, [c_vp]),
+        "cm_ctx_selftest_wait": (c_int, [c_vp, c_vp]),
         "cm_engine_create": (c_int, [c_int, c_i32, c_i64, c_i32, c_i64, c_i64, ctypes.POINTER(c_vp)]),
         "cm_engine_poll": (c_int, [c_vp, c_i64, _I32P]),
         "cm_engine_destroy": (None, [c_vp]),

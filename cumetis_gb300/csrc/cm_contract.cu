@@ -41,7 +41,10 @@ namespace {
 #define CM_TILE_THREADS 256
 #endif
 constexpr int kTileThreads = CM_TILE_THREADS;     // threads per contraction tile
-constexpr int kTileE = 4;
+#ifndef CM_TILE_E
+#define CM_TILE_E 4
+#endif
+constexpr int kTileE = CM_TILE_E;                 // keys per lane in the tile sort's register runs
 constexpr int kTileDiag = 512;                    // D
 constexpr int kLongThr = 1024;                    // rows longer than this take the long path
 constexpr int kTileCap = kTileDiag + kLongThr;    // max entries in a tile (multiple of kTileE)

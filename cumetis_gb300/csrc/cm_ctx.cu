@@ -123,6 +123,13 @@ bool bad_graph(const cm_graph *g) {
          (g->nvtxs > 0 && (!g->xadj || !g->vwgt)) || (g->nedges > 0 && (!g->adjncy || !g->adjwgt));
 }
 
+// One warp resolving look-back tile 1 while tile 0 never publishes: the
+// production wait (lookback_resolve) must give up after its time limit and
+// record CM_ERR_LIMIT.
+__global__ void k_selftest_wait(unsigned long long *status, DevStatus *st) {
+  lookback_exclusive(status, 1, 1ull, st);
+}
+
 __global__ void k_sum_i32(const int *a, long long n, unsigned long long *out) {
   unsigned long long s = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -204,6 +211,21 @@ extern "C" void cm_ctx_destroy(cm_ctx *ctx) {
 }
 
 extern "C" void *cm_ctx_stream(const cm_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+extern "C" int cm_ctx_selftest_wait(cm_ctx *ctx, void *stream) {
+  if (!ctx) return cm_fail(CM_ERR_INVALID, "cm_ctx_selftest_wait: null context");
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  ws_reset(ctx);
+  if ((rc = ws_ensure(ctx, 4096))) return rc;
+  unsigned long long *status = (unsigned long long *)ws_take(ctx, 64);
+  cudaMemsetAsync(status, 0, 64, s);
+  k_selftest_wait<<<1, 32, 0, s>>>(status, ctx->d_status);
+  ctx->launches++;
+  if ((rc = check_launch(ctx, "selftest wait"))) return rc;
+  return take_device_error(ctx, s);
+}
 
 extern "C" int cm_ctx_reserve(cm_ctx *ctx, int64_t nvtxs, int64_t nedges) {
   if (!ctx || nvtxs < 0 || nedges < 0) return cm_fail(CM_ERR_INVALID, "cm_ctx_reserve: bad arguments");

@@ -118,6 +118,11 @@ int cm_ctx_sync(cm_ctx *ctx, void *stream);
 /* The context's own non-blocking stream (a cudaStream_t), used by entry
  * points without a stream argument (cm_part_graph). */
 void *cm_ctx_stream(const cm_ctx *ctx);
+/* Failure-path check without a fault: runs the library's bounded device wait
+ * (the decoupled look-back) on a predecessor that never publishes.  Returns
+ * CM_ERR_LIMIT after the wait's time limit (about 2 s); the context stays
+ * usable. */
+int cm_ctx_selftest_wait(cm_ctx *ctx, void *stream);
 /* Number of kernels this context has launched since creation. */
 int64_t cm_ctx_launch_count(const cm_ctx *ctx);
 
