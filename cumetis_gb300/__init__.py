@@ -93,6 +93,7 @@ def _declare(L):
                                 c_i32, c_i32, G]),
         "cm_gen_rgg": (c_int, [c_i32, ctypes.c_double, ctypes.c_uint64, G]),
         "cm_read_graph": (c_int, [ctypes.c_char_p, G]),
+        "cm_read_mtx": (c_int, [ctypes.c_char_p, G]),
         "cm_write_graph": (c_int, [ctypes.c_char_p, G]),
         "cm_write_partition": (c_int, [ctypes.c_char_p, c_i32, c_i32, _I32P]),
         "cm_edge_cut": (c_i64, [G, _I32P]),
@@ -265,6 +266,12 @@ def gen_rgg(n, mean_degree=8.0, seed=1):
 
 def read_graph(path):
     return _gen(lib().cm_read_graph, path.encode())
+
+
+def read_mtx(path):
+    """MatrixMarket coordinate matrix -> Graph (pattern of A + A^T without the
+    diagonal, unit weights; the reference's mtx_to_graph)."""
+    return _gen(lib().cm_read_mtx, path.encode())
 
 
 def write_partition(graph_path, nparts, part):

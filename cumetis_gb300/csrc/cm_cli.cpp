@@ -3,6 +3,12 @@
 //
 //   cuMetis <graph> <k> [--seed S] [--device D] [--coarsen-to N] [--passes P]
 //                       [--lex-ties] [--no-write]
+//   cuMetis convert <matrix.mtx> [<out.graph>]
+//
+// A <graph> ending in .mtx is read as a MatrixMarket matrix (the pattern of
+// A + A^T without the diagonal).  `convert` writes that graph as a METIS file,
+// by default <matrix>.graph -- the reference's mtx_to_graph builds this name
+// without a terminating NUL, which garbles it.
 //
 // Reads a METIS .graph file, partitions it into k parts (cm_part_graph),
 // prints the reference's report lines (timings, edge cut) plus the imbalance,
@@ -13,6 +19,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "cm.h"
@@ -20,12 +27,41 @@
 static int usage(const char *argv0) {
   std::fprintf(stderr,
                "usage: %s <graph> <k> [--seed S] [--device D] [--coarsen-to N] [--passes P] [--lex-ties] "
-               "[--no-write]\n",
-               argv0);
+               "[--no-write]\n       %s convert <matrix.mtx> [<out.graph>]\n",
+               argv0, argv0);
   return 2;
 }
 
+static bool ends_with(const char *s, const char *suffix) {
+  const size_t n = std::strlen(s), k = std::strlen(suffix);
+  return n >= k && std::strcmp(s + n - k, suffix) == 0;
+}
+
+static int read_input(const char *path, cm_graph *g) {
+  return ends_with(path, ".mtx") ? cm_read_mtx(path, g) : cm_read_graph(path, g);
+}
+
+static int convert(int argc, char **argv) {
+  if (argc < 3 || argc > 4) return usage(argv[0]);
+  const char *in = argv[2];
+  std::string out = argc == 4 ? std::string(argv[3]) : std::string(in);
+  if (argc == 3) {
+    if (ends_with(in, ".mtx")) out.resize(out.size() - 4);
+    out += ".graph";
+  }
+  cm_graph g{};
+  if (cm_read_mtx(in, &g) != CM_OK || cm_write_graph(out.c_str(), &g) != CM_OK) {
+    std::fprintf(stderr, "%s\n", cm_last_error());
+    cm_graph_free(&g);
+    return 1;
+  }
+  std::printf("%s: %d vertices, %lld edges\n", out.c_str(), g.nvtxs, (long long)(g.nedges / 2));
+  cm_graph_free(&g);
+  return 0;
+}
+
 int main(int argc, char **argv) {
+  if (argc >= 2 && !std::strcmp(argv[1], "convert")) return convert(argc, argv);
   if (argc < 3) return usage(argv[0]);
   const char *path = argv[1];
   const int k = std::atoi(argv[2]);
@@ -44,7 +80,7 @@ int main(int argc, char **argv) {
     else return usage(argv[0]);
   }
   cm_graph g{};
-  if (cm_read_graph(path, &g) != CM_OK) {
+  if (read_input(path, &g) != CM_OK) {
     std::fprintf(stderr, "%s\n", cm_last_error());
     return 1;
   }

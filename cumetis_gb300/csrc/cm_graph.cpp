@@ -6,6 +6,8 @@
 //                                              error cases; nedges *= 2)
 //   cuMetis.cu:3856-3870  cuMetis_writetofile (<graph>.part.<k>, one id per line)
 //   cuMetis.cu:356-366    cuMetis_computecut  (sum of cut entries / 2)
+//   mtx_to_graph.c        MatrixMarket -> graph: the pattern of A + A^T
+//                         without the diagonal, unit weights
 // The generators have no reference counterpart: they produce the synthetic
 // workloads (meshes, R-MAT, random geometric graphs) with counter-based
 // randomness, so the same (sizes, seed) give the same graph on any host and
@@ -18,6 +20,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
+#include <utility>
 #include <vector>
 
 #ifdef _OPENMP
@@ -408,6 +412,68 @@ extern "C" int cm_write_graph(const char *path, const cm_graph *g) {
   int bad = ferror(fp);
   fclose(fp);
   return bad ? cm_fail(CM_ERR_IO, "write_graph: write error on %s", path) : CM_OK;
+}
+
+// MatrixMarket coordinate file -> graph with the pattern of A + A^T minus the
+// diagonal, rows sorted, unit weights (what mtx_to_graph.c writes: it merges
+// each row of A with the same row of A^T and drops i == j).  Symmetric,
+// skew-symmetric and Hermitian files list one triangle; both directions are
+// added either way.  Values are ignored.  The matrix must be square.
+extern "C" int cm_read_mtx(const char *path, cm_graph *out) {
+  if (!path || !out) return cm_fail(CM_ERR_INVALID, "read_mtx: null argument");
+  *out = cm_graph{};
+  FILE *fp = fopen(path, "r");
+  if (!fp) return cm_fail(CM_ERR_IO, "file: %s, mode: r: %s", path, strerror(errno));
+  char line[4096];
+  if (!fgets(line, sizeof line, fp) || strncmp(line, "%%MatrixMarket", 14) != 0) {
+    fclose(fp);
+    return cm_fail(CM_ERR_IO, "read_mtx: %s: missing %%%%MatrixMarket header", path);
+  }
+  if (!strstr(line, "coordinate")) {
+    fclose(fp);
+    return cm_fail(CM_ERR_IO, "read_mtx: %s: only coordinate matrices are graphs", path);
+  }
+  long long nr = 0, nc = 0, nnz = 0;
+  while (fgets(line, sizeof line, fp)) {
+    if (line[0] == '%') continue;
+    if (sscanf(line, "%lld %lld %lld", &nr, &nc, &nnz) == 3) break;
+    nr = -1;
+    break;
+  }
+  if (nr <= 0 || nr != nc || nnz < 0 || nr >= INT32_MAX) {
+    fclose(fp);
+    return cm_fail(CM_ERR_IO, "read_mtx: %s: bad or non-square size line", path);
+  }
+  std::vector<std::pair<int32_t, int32_t>> e;
+  e.reserve((size_t)nnz * 2);
+  for (long long k = 0; k < nnz; ++k) {
+    long long i, j;
+    if (!fgets(line, sizeof line, fp) || sscanf(line, "%lld %lld", &i, &j) != 2 || i < 1 || j < 1 || i > nr ||
+        j > nr) {
+      fclose(fp);
+      return cm_fail(CM_ERR_IO, "read_mtx: %s: bad entry %lld", path, k + 1);
+    }
+    if (i == j) continue;
+    e.emplace_back((int32_t)(i - 1), (int32_t)(j - 1));
+    e.emplace_back((int32_t)(j - 1), (int32_t)(i - 1));
+  }
+  fclose(fp);
+  std::sort(e.begin(), e.end());
+  e.erase(std::unique(e.begin(), e.end()), e.end());
+  if (e.size() >= (size_t)INT32_MAX) return cm_fail(CM_ERR_UNSUPPORTED, "read_mtx: %s: too many entries", path);
+  int rc = cm_graph_alloc((int32_t)nr, (int32_t)e.size(), out);
+  if (rc) return rc;
+  std::fill(out->xadj, out->xadj + nr + 1, 0);
+  for (size_t k = 0; k < e.size(); ++k) {
+    out->xadj[e[k].first + 1]++;
+    out->adjncy[k] = e[k].second;
+    out->adjwgt[k] = 1;
+  }
+  for (long long v = 0; v < nr; ++v) {
+    out->xadj[v + 1] += out->xadj[v];
+    out->vwgt[v] = 1;
+  }
+  return CM_OK;
 }
 
 extern "C" int cm_write_partition(const char *graph_path, int32_t nparts, int32_t nvtxs, const int32_t *part) {

@@ -16,6 +16,7 @@
  *   cuMetis.cu:3712  cuMetis_readgraph(filename)                       -> cm_read_graph
  *   cuMetis.cu:3856  cuMetis_writetofile(fname, part, n, nparts)       -> cm_write_partition
  *   cuMetis.cu:356   cuMetis_computecut(graph, where)                  -> cm_edge_cut
+ *   mtx_to_graph.c   main (MatrixMarket -> .graph)                     -> cm_read_mtx + cm_write_graph
  *
  * Conventions
  *   - Every function returns CM_OK (0) or a CM_ERR_* code; none calls exit().
@@ -96,6 +97,9 @@ int cm_gen_rgg(int32_t n, double mean_degree, uint64_t seed, cm_graph *out);
 /* METIS .graph IO (formats 0/1/10/11 and the 100s digit, as cuMetis.cu:3712). */
 int cm_read_graph(const char *path, cm_graph *out);
 int cm_write_graph(const char *path, const cm_graph *g);
+/* MatrixMarket coordinate file (square) -> graph with the pattern of A + A^T
+ * without the diagonal, unit weights (the reference's mtx_to_graph.c). */
+int cm_read_mtx(const char *path, cm_graph *out);
 /* Writes "<graph_path>.part.<nparts>", one part id per line (cuMetis.cu:3856). */
 int cm_write_partition(const char *graph_path, int32_t nparts, int32_t nvtxs, const int32_t *part);
 /* Edge cut (sum of cut edge weights / 2) and max part weight * nparts / total. */

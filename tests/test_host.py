@@ -160,3 +160,52 @@ def test_engine_without_device_fails_loudly():
     with pytest.raises(cm.CMError) as e:
         cm.Engine(0, workers=2)
     assert e.value.code == cm.CM_ERR_UNSUPPORTED
+
+
+MTX_CASES = {
+    "symmetric": ("%%MatrixMarket matrix coordinate real symmetric\n% c\n5 5 6\n1 1 1\n2 1 1\n3 2 1\n5 3 1\n4 4 2\n5 1 3\n",
+                  {(0, 1), (1, 2), (2, 4), (0, 4)}),
+    "general": ("%%MatrixMarket matrix coordinate pattern general\n4 4 5\n1 2\n2 1\n3 4\n1 1\n4 2\n",
+                {(0, 1), (2, 3), (1, 3)}),
+    "skew": ("%%MatrixMarket matrix coordinate integer skew-symmetric\n3 3 2\n2 1 -4\n3 1 7\n", {(0, 1), (0, 2)}),
+}
+
+
+@pytest.mark.parametrize("name", sorted(MTX_CASES))
+def test_mtx_reader(tmp_path, name):
+    text, und = MTX_CASES[name]
+    p = tmp_path / (name + ".mtx")
+    p.write_text(text)
+    g = cm.read_mtx(str(p))
+    n = int(text.split("\n")[1 if not text.split("\n")[1].startswith("%") else 2].split()[0])
+    pairs = sorted({(a, b) for a, b in und} | {(b, a) for a, b in und})
+    xadj = np.zeros(n + 1, np.int64)
+    for a, _ in pairs:
+        xadj[a + 1] += 1
+    np.testing.assert_array_equal(g.xadj, np.cumsum(xadj))
+    np.testing.assert_array_equal(g.adjncy, [b for _, b in pairs])
+    assert (g.adjwgt == 1).all() and (g.vwgt == 1).all()
+
+
+@pytest.mark.parametrize("text", ["%%MatrixMarket matrix array real general\n2 2\n1\n2\n3\n4\n",
+                                  "%%MatrixMarket matrix coordinate real general\n3 4 1\n1 2 1\n",
+                                  "%%MatrixMarket matrix coordinate real general\n3 3 2\n1 2 1\n",
+                                  "not a header\n3 3 0\n"])
+def test_mtx_reader_errors(tmp_path, text):
+    p = tmp_path / "bad.mtx"
+    p.write_text(text)
+    with pytest.raises(cm.CMError) as e:
+        cm.read_mtx(str(p))
+    assert e.value.code == cm.CM_ERR_IO
+
+
+def test_cli_convert(tmp_path):
+    p = tmp_path / "m.mtx"
+    p.write_text(MTX_CASES["symmetric"][0])
+    exe = os.path.join(os.path.dirname(cm.LIB_PATH), "cuMetis")
+    r = subprocess.run([exe, "convert", str(p)], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    assert r.returncode == 0, r.stderr
+    g = cm.read_graph(str(tmp_path / "m.graph"))
+    h = cm.read_mtx(str(p))
+    np.testing.assert_array_equal(g.xadj, h.xadj)
+    np.testing.assert_array_equal(g.adjncy, h.adjncy)
