@@ -132,11 +132,15 @@ __device__ __forceinline__ int hash_get(const K *hk, const int *hw, unsigned hma
   return 0;
 }
 
-// Table size for n keys: the power of two >= 2n (at least 64, at most cap);
-// returns log2 of it.
+// Table size for n keys: the power of two >= kHashSlack2 * n / 2 (load at
+// most 2 / kHashSlack2; at least 64 slots, at most the cap); returns log2.
+#ifndef CM_HASH_SLACK2
+#define CM_HASH_SLACK2 4
+#endif
+constexpr int kHashSlack2 = CM_HASH_SLACK2;
 __device__ __forceinline__ int hash_log2(int n, int cap_log2) {
   int lg = 6;
-  while (lg < cap_log2 && (1 << lg) < 2 * n) ++lg;
+  while (lg < cap_log2 && 2 * (1 << lg) < kHashSlack2 * n) ++lg;
   return lg;
 }
 

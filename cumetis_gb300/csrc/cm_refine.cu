@@ -42,16 +42,24 @@ constexpr int kRefWarps = kRefThreads / 32;
 constexpr int kSmemParts = 1024;          // per-warp part accumulators in shared memory up to this k
 constexpr int kSortBlock = 1024;          // boundary entries per counting-sort block
 
-// Part weights (atomics, shared-memory histogram when k is small).
-__global__ void k_part_weights(int n, const int *__restrict__ where, const int *__restrict__ vwgt, int nparts,
-                               int *__restrict__ pwgts) {
+// Part weights (atomics, shared-memory histogram when k is small).  With a
+// coarser level given (cmap, cwhere), the kernel first projects it:
+// where[v] = cwhere[cmap[v]] (cuMetis_kway_project fused into the pass).
+__global__ void k_part_weights(int n, int *__restrict__ where, const int *__restrict__ vwgt, int nparts,
+                               int *__restrict__ pwgts, const int *__restrict__ cmap, const int *__restrict__ cwhere) {
   extern __shared__ int h[];
   const bool sh = nparts <= 8192;
   if (sh)
     for (int i = threadIdx.x; i < nparts; i += blockDim.x) h[i] = 0;
   __syncthreads();
   for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
-    const int p = where[v];
+    int p;
+    if (cmap) {
+      p = cwhere[cmap[v]];
+      where[v] = p;
+    } else {
+      p = where[v];
+    }
     if (sh) atomicAdd(&h[p], vwgt[v]);
     else atomicAdd(&pwgts[p], vwgt[v]);
   }
@@ -352,13 +360,14 @@ int take_refine_ws(cm_ctx *ctx, int64_t n, int nparts, RefineWs &w) {
 }
 
 // One refinement pass over level graph g (device) with partition where.
-int refine_pass(cm_ctx *ctx, const cm_graph &g, int nparts, int32_t *where, RefineWs &w, cudaStream_t s) {
+int refine_pass(cm_ctx *ctx, const cm_graph &g, int nparts, int32_t *where, RefineWs &w, cudaStream_t s,
+                const int32_t *proj_cmap = nullptr, const int32_t *proj_cwhere = nullptr) {
   const int n = g.nvtxs;
   if (n == 0) return CM_OK;
   const int sms = ctx->num_sms;
   cudaMemsetAsync(w.pwgts, 0, (size_t)nparts * 4, s);
   const size_t hsh = nparts <= 8192 ? (size_t)nparts * 4 : 0;
-  k_part_weights<<<sms * 4, 256, hsh, s>>>(n, where, g.vwgt, nparts, w.pwgts);
+  k_part_weights<<<sms * 4, 256, hsh, s>>>(n, where, g.vwgt, nparts, w.pwgts, proj_cmap, proj_cwhere);
   // tpwgts = 1.0 / nparts rounded to float, as cuMetis_set_graph_admin stores it (cu:384)
   k_part_bounds<<<1, 1024, 0, s>>>(nparts, (float)(1.0 / nparts), w.pwgts, w.maxw, w.minw);
   if (nparts <= kSmemParts) {
@@ -559,12 +568,12 @@ extern "C" int cm_part_graph(cm_ctx *ctx, int32_t nvtxs, const int32_t *xadj, co
   cudaMemcpyAsync(wl[L - 1], cwhere.data(), (size_t)lg[L - 1].nvtxs * 4, cudaMemcpyHostToDevice, s);
   const int passes = std::max(1, P.refine_passes);
   for (int l = L - 1; l >= 0; --l) {
-    if (l < L - 1) {
-      k_project<<<ctx->num_sms * 4, 256, 0, s>>>(lg[l].nvtxs, lcmap[l], wl[l + 1], wl[l]);
-      ctx->launches++;
+    // the first pass of a finer level projects the coarser partition itself
+    for (int p = 0; p < passes; ++p) {
+      const bool proj = l < L - 1 && p == 0;
+      if ((rc = refine_pass(ctx, lg[l], nparts, wl[l], w, s, proj ? lcmap[l] : nullptr, proj ? wl[l + 1] : nullptr)))
+        return finish(rc);
     }
-    for (int p = 0; p < passes; ++p)
-      if ((rc = refine_pass(ctx, lg[l], nparts, wl[l], w, s))) return finish(rc);
   }
   if ((rc = take_device_error(ctx, s))) return finish(rc);
   int64_t cut = 0;
