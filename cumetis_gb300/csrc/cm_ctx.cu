@@ -4,7 +4,7 @@
 //
 // Differences from the reference's level loop, by design:
 //   - no cudaMalloc/cudaFree inside a level: per-level graphs come from the
-//     stream-ordered pool (cudaMallocAsync) and scratch from the context
+//     context's stream-ordered pool (cudaMallocFromPoolAsync) and scratch from the context
 //     workspace, sized once for the input;
 //   - no host round trips inside a level: matching, cmap, contraction run
 //     back to back on one stream; one 8-byte readback of (n', m') per level
@@ -175,11 +175,16 @@ extern "C" int cm_ctx_create(int device, cm_ctx **out) {
   }
   if (!rc) rc = cuda_status(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming), "fork event");
   if (!rc) {
-    // Keep freed level buffers in the stream-ordered pool between calls.
-    cudaMemPool_t pool;
-    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    // The context's own pool; freed level buffers stay in it between calls.
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    rc = cuda_status(cudaMemPoolCreate(&ctx->pool, &props), "memory pool");
+    if (!rc) {
       uint64_t thr = UINT64_MAX;
-      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+      cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &thr);
     }
   }
   if (rc) {
@@ -207,6 +212,7 @@ extern "C" void cm_ctx_destroy(cm_ctx *ctx) {
   }
   if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->pool) cudaMemPoolDestroy(ctx->pool);  // blocks still held by hierarchies keep it alive until freed
   delete ctx;
 }
 
@@ -377,12 +383,12 @@ namespace {
 size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // One pooled block holding xadj(n+1), vwgt(n), adjncy(m), adjwgt(m), match(n), cmap(n).
-int alloc_level(cm_level &L, int64_t n, int64_t m, cudaStream_t s) {
+int alloc_level(cm_level &L, int64_t n, int64_t m, cudaMemPool_t pool, cudaStream_t s) {
   const size_t bx = align256((n + 1) * 4), bv = align256(std::max<int64_t>(n, 1) * 4),
                be = align256(std::max<int64_t>(m, 1) * 4);
   const size_t total = bx + bv + 2 * be + 2 * bv;
   char *p = nullptr;
-  int rc = cuda_status(cudaMallocAsync((void **)&p, total, s), "level alloc");
+  int rc = cuda_status(cudaMallocFromPoolAsync((void **)&p, total, pool, s), "level alloc");
   if (rc) return rc;
   L.block = p;
   L.g.xadj = (int32_t *)p;
@@ -431,7 +437,7 @@ extern "C" int cm_coarsen(cm_ctx *ctx, const cm_graph *g, int input_on_device, c
     // match + cmap for level 0 from the pool
     char *p = nullptr;
     const size_t bv = align256(std::max<int64_t>(n0, 1) * 4);
-    if ((rc = cuda_status(cudaMallocAsync((void **)&p, 2 * bv, s), "level alloc"))) return fail(rc);
+    if ((rc = cuda_status(cudaMallocFromPoolAsync((void **)&p, 2 * bv, ctx->pool, s), "level alloc"))) return fail(rc);
     L0.block = p;
     L0.match = (int32_t *)p;
     L0.cmap = (int32_t *)(p + bv);
@@ -445,7 +451,7 @@ extern "C" int cm_coarsen(cm_ctx *ctx, const cm_graph *g, int input_on_device, c
       return fail(rc);
     tvwgt = (int64_t)hs;
   } else {
-    if ((rc = alloc_level(L0, n0, m0, s))) return fail(rc);
+    if ((rc = alloc_level(L0, n0, m0, ctx->pool, s))) return fail(rc);
     L0.g.nvtxs = (int32_t)n0;
     L0.g.nedges = (int32_t)m0;
     cudaMemcpyAsync(L0.g.xadj, g->xadj, (n0 + 1) * 4, cudaMemcpyHostToDevice, s);
@@ -465,7 +471,7 @@ extern "C" int cm_coarsen(cm_ctx *ctx, const cm_graph *g, int input_on_device, c
     cm_level &F = h->levels.back();
     const int64_t n = F.g.nvtxs, m = F.g.nedges;
     cm_level C;
-    if ((rc = alloc_level(C, n, m, s))) return fail(rc);
+    if ((rc = alloc_level(C, n, m, ctx->pool, s))) return fail(rc);
     ctx->ws_used = level_ws_off;
     if ((rc = launch_match(ctx, &F.g, h->maxvwgt, params->match_mode, F.match, s))) {
       cudaFreeAsync(C.block, s);

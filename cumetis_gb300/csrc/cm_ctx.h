@@ -30,6 +30,10 @@ struct cm_ctx {
   // the context's own stream (non-blocking), used by calls without a stream
   // argument (cm_part_graph)
   cudaStream_t stream = nullptr;
+  // the context's own stream-ordered memory pool for level graphs and
+  // partitions: blocks freed by one context are reused only by that context,
+  // so contexts running side by side never wait on each other's streams
+  cudaMemPool_t pool = nullptr;
   // internal streams/events for concurrent contraction stages
   cudaStream_t aux[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t fork_ev = nullptr, join_ev[3] = {nullptr, nullptr, nullptr};

@@ -542,7 +542,7 @@ extern "C" int cm_part_graph(cm_ctx *ctx, int32_t nvtxs, const int32_t *xadj, co
   int64_t total_n = 0;
   for (int l = 0; l < L; ++l) total_n += lg[l].nvtxs;
   int32_t *wbuf = nullptr;
-  if ((rc = cuda_status(cudaMallocAsync((void **)&wbuf, (size_t)std::max<int64_t>(total_n, 1) * 4, s), "where alloc"))) {
+  if ((rc = cuda_status(cudaMallocFromPoolAsync((void **)&wbuf, (size_t)std::max<int64_t>(total_n, 1) * 4, ctx->pool, s), "where alloc"))) {
     cm_hierarchy_free(h);
     return rc;
   }
