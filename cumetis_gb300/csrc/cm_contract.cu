@@ -370,22 +370,30 @@ k_count_scan(const int *__restrict__ ucount, const int *d_cn, int *__restrict__ 
 }
 
 // Copies the short rows' unique entries from the stage to their final place
-// cxadj[c] (one block per tile, one thread per entry).
-constexpr int kCopyThreads = 128;
+// cxadj[c]: one block per group of kCopyGroup consecutive tiles, one thread
+// per entry.
+#ifndef CM_COPY_GROUP
+#define CM_COPY_GROUP 1
+#endif
+#ifndef CM_COPY_THREADS
+#define CM_COPY_THREADS 128
+#endif
+constexpr int kCopyThreads = CM_COPY_THREADS, kCopyGroup = CM_COPY_GROUP;
+constexpr int kCopyRows = kTileDiag * kCopyGroup;
 __global__ void __launch_bounds__(kCopyThreads)
 k_copy_tiles(const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
              const int *__restrict__ ucount, const int *__restrict__ cxadj, const int2 *__restrict__ stage,
              int *__restrict__ cadjncy, int *__restrict__ cadjwgt) {
-  __shared__ int s_pre[kTileDiag + 1], s_src[kTileDiag], s_dst[kTileDiag], s_scan[kCopyThreads / 32 + 1];
+  __shared__ int s_pre[kCopyRows + 1], s_src[kCopyRows], s_dst[kCopyRows], s_scan[kCopyThreads / 32 + 1];
   const int tid = threadIdx.x;
   const int nc = *d_cn;
   const long long dend = (long long)nc + eoff[nc];
   const long long last = dend / kTileDiag;
-  const int tile = blockIdx.x;
-  const int clo = tile <= last ? first_row[tile] : nc;
-  const int chi = tile + 1 <= last ? first_row[tile + 1] : nc;
-  const int R = max(0, min(kTileDiag, chi - clo));
-  constexpr int kRowsPerThread = kTileDiag / kCopyThreads;
+  const long long t0 = (long long)blockIdx.x * kCopyGroup, t1 = t0 + kCopyGroup;
+  const int clo = t0 <= last ? first_row[t0] : nc;
+  const int chi = t1 <= last ? first_row[t1] : nc;
+  const int R = max(0, min(kCopyRows, chi - clo));
+  constexpr int kRowsPerThread = kCopyRows / kCopyThreads;
   int cnt[kRowsPerThread];
   int mysum = 0;
 #pragma unroll
@@ -880,7 +888,7 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
                                                  stage0, stage1, chunk_cnt, ucount, coarse->xadj, coarse->adjncy,
                                                  coarse->adjwgt);
   cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
-  k_copy_tiles<<<(unsigned)ntiles, kCopyThreads, 0, s>>>(eoff, d_sizes, first_row, ucount, coarse->xadj, stage1,
+  k_copy_tiles<<<(unsigned)((ntiles + kCopyGroup - 1) / kCopyGroup), kCopyThreads, 0, s>>>(eoff, d_sizes, first_row, ucount, coarse->xadj, stage1,
                                                          coarse->adjncy, coarse->adjwgt);
   ctx->launches += 2;
   cudaStreamWaitEvent(s, ctx->join_ev[0], 0);
