@@ -236,6 +236,22 @@ def run_batch(args):
     _, cuts, st = cm.part_batch(graphs, ks, workers=args.workers)
     dt = time.perf_counter() - t1
     clk = clocks.stop()
+    # The plain per-graph launch for comparison: one context, one graph at a
+    # time (cm_part_graph), on a sample of the same batch.
+    import torch
+    ctx1 = cm.Context(0)
+    sample = list(range(0, len(graphs), max(1, len(graphs) // 64)))
+    for i in sample[:4]:
+        ctx1.part_graph(graphs[i], ks[i])
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    for i in sample:
+        ctx1.part_graph(graphs[i], ks[i])
+    plain_dt = time.perf_counter() - t2
+    ctx1.close()
+    plain_rate = len(sample) / plain_dt
+    # the sample's share of the batch's work, to compare rates on equal work
+    sample_m = sum(graphs[i].nedges for i in sample)
     n_sum = int(sum(g.nvtxs for g in graphs))
     m_sum = int(sum(g.nedges for g in graphs))
     imb = [float(np.bincount(p, minlength=k).max() * k / g.nvtxs) for g, p, k in
@@ -251,6 +267,9 @@ def run_batch(args):
                                          "initial_partition": st["sum_init_ms"] / len(graphs),
                                          "refine_project": st["sum_uncoarsen_ms"] / len(graphs)}},
             "edges_per_s": m_sum / dt, "mean_edge_cut": float(np.mean(cuts)),
+            "plain_per_graph": {"partitions_per_s": plain_rate, "edges_per_s": sample_m / plain_dt,
+                                "sample_graphs": len(sample),
+                                "batch_speedup_edges": (m_sum / dt) / (sample_m / plain_dt)},
             "mean_imbalance_first64": float(np.mean(imb)), "clocks": clk, "gpu_launches": None,
             "e2e": {"value": len(graphs) / dt, "unit": "partitions/s",
                     "h2d_bytes_per_step": int(4 * (2 * n_sum + len(graphs) + 2 * m_sum)),

@@ -63,3 +63,30 @@ def test_engine_many_jobs_and_errors():
     with pytest.raises(cm.CMError):
         e.submit(gs[0], 0)
     e.close()
+
+
+def test_served_result_same_alone_and_in_the_mix(ctx):
+    """A request's result does not depend on what else the engine runs: with
+    two parts it is identical alone and among 40 concurrent requests; with
+    more parts (whose refinement groups race on part weights, as in the
+    reference) the edge cut stays within 3% and the balance window holds."""
+    target2 = cm.gen_grid2d(150, 120)
+    target16 = cm.gen_rmat(14, 16, seed=7)
+    alone2, cut_alone2, _ = ctx.part_graph(target2, 2)
+    alone16, cut_alone16, _ = ctx.part_graph(target16, 16)
+    e = cm.Engine(0, workers=8)
+    mix = [cm.gen_rgg(3000 + 500 * i, 8.0, seed=i) for i in range(40)]
+    jobs = [e.submit(g, 2 + i % 30) for i, g in enumerate(mix[:20])]
+    j2 = e.submit(target2, 2)
+    j16 = e.submit(target16, 16)
+    jobs += [e.submit(g, 2 + i % 30) for i, g in enumerate(mix[20:])]
+    p2, c2, _ = e.wait(j2)
+    p16, c16, _ = e.wait(j16)
+    for j in jobs:
+        e.wait(j)
+    e.close()
+    np.testing.assert_array_equal(p2, alone2)
+    assert c2 == cut_alone2
+    assert abs(c16 - cut_alone16) <= 0.03 * cut_alone16
+    pw = np.bincount(p16, weights=target16.vwgt, minlength=16)
+    assert pw.max() * 16 / target16.vwgt.sum() < 1.10
