@@ -384,7 +384,7 @@ def main():
                     help="matching tie order: 1 = edge hash (default), 0 = lower vertex id")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) measurement")
-    ap.add_argument("--e2e-pipes", type=int, default=3, help="host threads (contexts) taking alternate e2e steps")
+    ap.add_argument("--e2e-pipes", type=int, default=4, help="host threads (contexts) taking alternate e2e steps")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_setup(args.gpus)
@@ -494,8 +494,8 @@ def main():
         # on host arrays + cm_hierarchy_read_level).  args.e2e_pipes host
         # threads, each with its own context (and stream), take alternate
         # steps, so one step's copies overlap another step's kernels; the
-        # host link (about 210 GB/s each way here) is otherwise idle while
-        # the GPU computes.
+        # host link (about 210 GB/s one way, 340 GB/s both ways at once) is
+        # otherwise idle while the GPU computes.
         import threading
         pin = {a: torch.empty(getattr(g, a).shape[0], dtype=torch.int32, pin_memory=True) for a in
                ("xadj", "adjncy", "adjwgt", "vwgt")}
