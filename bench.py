@@ -528,7 +528,7 @@ def main():
             e2e_step(i)
         barrier(ws)
         torch.cuda.synchronize()
-        e2e_steps = max(pipes, (args.steps // 4) // pipes * pipes)
+        e2e_steps = max(pipes, args.steps // pipes * pipes)
         t0 = time.perf_counter()
         ths = [threading.Thread(target=run, args=(i, e2e_steps // pipes)) for i in range(pipes)]
         for t in ths:

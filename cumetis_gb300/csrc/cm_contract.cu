@@ -15,20 +15,17 @@
 // Work split by expanded coarse-row length L = deg(leader) + deg(follower):
 //   L <= kLongThr : contraction tiles.  Tile k owns the rows whose diagonal
 //                   c + eoff[c] lies in [kD, (k+1)D) (D = kTileDiag), so a tile
-//                   holds <= D rows and < D + kLongThr entries.  Two passes:
-//                   the count pass gathers the tile's entries and counts each
-//                   row's distinct coarse ids with a shared-memory hash set; a
-//                   scan of the counts gives cxadj (the "one more scan"); the
-//                   emit pass gathers again, sorts by (row, coarse id) with a
-//                   block merge sort, merges duplicates and writes each entry
-//                   once to its final place.
-//   L >  kLongThr : long rows, beside the count pass on auxiliary streams.
-//                   Rows up to kChunk entries: one block sorts and merges a
-//                   row (three size classes).  Longer rows: chunks of kChunk
-//                   entries are sorted in shared memory into a global stage,
-//                   merged pairwise (merge path, all blocks cooperating, one
-//                   grid barrier per pass) and deduplicated.  Their unique
-//                   entries are copied out beside the emit pass.
+//                   holds <= D rows and < D + kLongThr entries.  One pass per
+//                   tile: gather, merge duplicates in a shared-memory hash set,
+//                   sort the unique (row, coarse id) keys, and write each row's
+//                   unique entries to a stage at its expanded offset eoff[c].
+//   L >  kLongThr : long rows, beside the tiles on auxiliary streams.  Rows up
+//                   to kChunk entries: one block merges and sorts a row (three
+//                   size classes).  Longer rows: chunks of kChunk entries are
+//                   sorted in shared memory into a global stage, merged pairwise
+//                   (merge path, one launch per pass) and deduplicated.
+// A scan of the rows' unique counts gives cxadj; two copy kernels then move
+// every row from the stage to its final place.
 #include <algorithm>
 
 #include "cm_ctx.h"
@@ -206,6 +203,7 @@ __device__ __forceinline__ int tile_rows(TileSmem<K> &S, int tile, int nc, long 
     if (tid == 0) record_error(st, CM_ERR_INVALID, ERR_SITE_BOUNDS);
     R = 0;
   }
+  if (R == 0) return 0;  // a tile inside a long row's diagonal span holds no row
   constexpr int kRowsPerThread = kTileDiag / kTileThreads;
   int lens[kRowsPerThread];
   int mysum = 0;
@@ -265,6 +263,11 @@ k_contract_tiles(const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
   int clo, R;
   if (tid == 0) S.ctr = 0;
   const int ntot = tile_rows(S, blockIdx.x, nc, dend, first_row, row_meta, eoff, clo, R, st);
+  if (ntot == 0) {  // no short-row entries (uniform): short rows here are empty
+    for (int r = tid; r < R; r += kTileThreads)
+      if (S.r_out[r] >= 0) ucount[clo + r] = 0;
+    return;
+  }
   const int lg = hash_log2(ntot, kTileHashLog2);
   const int hsize = 1 << lg, shift = 64 - lg;
   const unsigned hmask = hsize - 1;
@@ -379,6 +382,7 @@ k_count_scan(const int *__restrict__ ucount, const int *d_cn, int *__restrict__ 
 #define CM_COPY_THREADS 128
 #endif
 constexpr int kCopyThreads = CM_COPY_THREADS, kCopyGroup = CM_COPY_GROUP;
+constexpr int kCopyBatch = 4;  // stage loads in flight per thread before their stores
 constexpr int kCopyRows = kTileDiag * kCopyGroup;
 __global__ void __launch_bounds__(kCopyThreads)
 k_copy_tiles(const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
@@ -393,6 +397,7 @@ k_copy_tiles(const int *__restrict__ eoff, const int *d_cn, const int *__restric
   const int clo = t0 <= last ? first_row[t0] : nc;
   const int chi = t1 <= last ? first_row[t1] : nc;
   const int R = max(0, min(kCopyRows, chi - clo));
+  if (R == 0) return;  // tiles inside a long row's diagonal span
   constexpr int kRowsPerThread = kCopyRows / kCopyThreads;
   int cnt[kRowsPerThread];
   int mysum = 0;
@@ -418,12 +423,27 @@ k_copy_tiles(const int *__restrict__ eoff, const int *d_cn, const int *__restric
     ex += cnt[i];
   }
   __syncthreads();
-  for (int o = tid; o < U; o += kCopyThreads) {
-    const int r = upper_bound_smem(s_pre, R, o) - 1;
-    const int k = o - s_pre[r];
-    const int2 e = stage[s_src[r] + k];
-    cadjncy[s_dst[r] + k] = e.x;
-    cadjwgt[s_dst[r] + k] = e.y;
+  for (int o0 = tid; o0 < U; o0 += kCopyBatch * kCopyThreads) {
+    int2 e[kCopyBatch];
+    int d[kCopyBatch];
+#pragma unroll
+    for (int u = 0; u < kCopyBatch; ++u) {
+      const int o = o0 + u * kCopyThreads;
+      d[u] = -1;
+      e[u] = make_int2(0, 0);
+      if (o < U) {
+        const int r = upper_bound_smem(s_pre, R, o) - 1;
+        const int k = o - s_pre[r];
+        e[u] = __ldcs(stage + s_src[r] + k);
+        d[u] = s_dst[r] + k;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kCopyBatch; ++u)
+      if (d[u] >= 0) {
+        cadjncy[d[u]] = e[u].x;
+        cadjwgt[d[u]] = e[u].y;
+      }
   }
 }
 
@@ -532,12 +552,12 @@ k_mid_rows(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const
 // in stage0 for the merge passes -- its unique entries (duplicates within the
 // chunk already merged, self loops dropped), then pad entries up to the
 // chunk's length, which sort after every coarse id and are skipped by the
-// dedup.
+// dedup.  chunk_np[q] = the merge passes the chunk's row needs.
 __global__ void __launch_bounds__(kChunkThreads, 1)
 k_long_sort(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
             const int *__restrict__ eoff, const int4 *__restrict__ row_meta, const int *__restrict__ long_list,
             const int *__restrict__ chunk_row, const unsigned long long *long_ctr, int2 *__restrict__ stage,
-            int *__restrict__ ucount) {
+            int *__restrict__ ucount, int *__restrict__ chunk_np) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MidSmem<kChunk> &S = *reinterpret_cast<MidSmem<kChunk> *>(smem_raw);
   const int nchunks = (int)(*long_ctr & 0xffffffffu);
@@ -549,6 +569,7 @@ k_long_sort(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, cons
     const int cs = j * kChunk;
     const int cnt = min(kChunk, md.w - cs);
     if (j == 0 && threadIdx.x == 0) ucount[c] = 0;  // the dedup adds the chunks' counts
+    if (threadIdx.x == 0) chunk_np[q] = merge_passes(md.w);
     int2 *dst = stage + eoff[c] + cs;
     const int U = unique_sorted_segment<kChunkThreads, kChunk>(S, c, md, cs, cnt, adjncy, adjwgt, cmap, dst);
     for (int t = U + threadIdx.x; t < cnt; t += kChunkThreads) dst[t] = make_int2((int)kPadId, 0);
@@ -557,76 +578,126 @@ k_long_sort(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, cons
 }
 
 // Items of merge(A[0..alen), B[0..blen)) taken from A among the first diag
-// outputs (A wins ties), on packed entries in global memory.
-__device__ __forceinline__ int merge_path_g(const int2 *A, int alen, const int2 *B, int blen, int diag) {
+// outputs (A wins ties), on packed entries in global memory: the first i in
+// [max(0, diag - blen), min(diag, alen)) with A[i] > B[diag - 1 - i], else the
+// upper end.  The predicate A[i] <= B[diag - 1 - i] holds on a prefix of the
+// range, so one warp probes 32 evenly spaced points per step and keeps the
+// gap between the last true and the first false probe: about log32 of the
+// range in dependent loads instead of log2.  All 32 lanes call it and get the
+// same result.
+__device__ __forceinline__ int merge_path_warp(const int2 *A, int alen, const int2 *B, int blen, int diag) {
+  const int lane = threadIdx.x & 31;
   int lo = diag > blen ? diag - blen : 0;
   int hi = diag < alen ? diag : alen;
   while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (pack_entry(__ldcg(&A[mid])) <= pack_entry(__ldcg(&B[diag - 1 - mid]))) lo = mid + 1;
-    else hi = mid;
+    const int stride = (hi - lo + 31) >> 5;  // >= 1; lane 31's probe may lie past hi
+    const int pos = lo + lane * stride;
+    const bool pred = pos < hi && pack_entry(__ldcg(&A[pos])) <= pack_entry(__ldcg(&B[diag - 1 - pos]));
+    const int t = __popc(__ballot_sync(0xffffffffu, pred));  // true probes: lanes 0 .. t-1
+    if (t == 0) {
+      hi = lo;  // false at lo
+    } else {
+      hi = min(hi, lo + t * stride);  // first false probe (or the end)
+      lo = lo + (t - 1) * stride + 1;  // one past the last true probe
+    }
   }
   return lo;
 }
 
 // One merge pass per launch: pass p merges run pairs of width kChunk << p
 // (launches beyond the longest row's last pass return at once; the host
-// launches the most passes a graph of m entries can need).  A block produces
-// one kChunk-sized block of
-// output: two threads find where it starts and ends in the two runs (merge
-// path over global memory), the block loads both windows into shared memory,
-// every thread merges kMergePer outputs there, and the block stores the
-// result coalesced.  Rows already a single run skip.
-constexpr int kMergeThreads = 512;
-constexpr int kMergePer = kChunk / kMergeThreads;  // 16
+// launches the most passes a graph of m entries can need).  Work items are
+// kMergeOut-sized pieces of output (kMergeSub per chunk).  A block first keeps
+// those of its items whose row still needs pass p (one load of chunk_np per
+// item, all at once), then per item: two warps find where it starts and ends
+// in the two runs (merge path over global memory, 32 probes per step), the
+// block loads both windows into shared memory, every thread merges kMergePer
+// outputs from there into registers, which then overwrite the window, and the
+// block stores the result coalesced.  Small blocks (several per SM) overlap
+// one another's load latencies.
+#ifndef CM_MERGE_THREADS
+#define CM_MERGE_THREADS 256
+#endif
+#ifndef CM_MERGE_OUT
+#define CM_MERGE_OUT 2048
+#endif
+constexpr int kMergeThreads = CM_MERGE_THREADS;
+constexpr int kMergeOut = CM_MERGE_OUT;                 // outputs per work item
+constexpr int kMergePer = kMergeOut / kMergeThreads;    // outputs per thread
+constexpr int kMergeSub = kChunk / kMergeOut;           // work items per chunk
+constexpr int kMergeBlocksPerSm = 65536 / (64 * kMergeThreads);
+static_assert(kMergePer * kMergeThreads == kMergeOut && kMergeSub * kMergeOut == kChunk, "merge tiling");
 struct MergeSmem {
-  unsigned long long win[padded_k<unsigned long long>(kChunk)];
-  unsigned long long out[padded_k<unsigned long long>(kChunk)];
-  int cut[4];
+  unsigned long long win[padded_k<unsigned long long>(kMergeOut)];  // the two input windows, then the output
+  int items[kMergeThreads];
+  int scan[kMergeThreads / 32 + 1];
+  int cut[2];
 };
 
-__global__ void __launch_bounds__(kMergeThreads)
+__global__ void __launch_bounds__(kMergeThreads, kMergeBlocksPerSm)
 k_long_merge(int p, const int *__restrict__ long_list, const int *__restrict__ chunk_row, const int *__restrict__ eoff,
-             const unsigned long long *long_ctr, int2 *stage0, int2 *stage1, const DevStatus *st) {
+             const unsigned long long *long_ctr, const int *__restrict__ chunk_np, int2 *stage0, int2 *stage1,
+             const DevStatus *st) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MergeSmem &S = *reinterpret_cast<MergeSmem *>(smem_raw);
-  const int nchunks = (int)(*long_ctr & 0xffffffffu);
   if (p >= merge_passes(st->max_row)) return;
-  {
-    const long long width = (long long)kChunk << p;
-    const int2 *src = (p & 1) ? stage1 : stage0;
-    int2 *dst = (p & 1) ? stage0 : stage1;
-    for (int q = blockIdx.x; q < nchunks; q += gridDim.x) {
+  const long long nitems = (long long)(int)(*long_ctr & 0xffffffffu) * kMergeSub;
+  const long long width = (long long)kChunk << p;
+  const int2 *src = (p & 1) ? stage1 : stage0;
+  int2 *dst = (p & 1) ? stage0 : stage1;
+  // the block's items are blockIdx.x + k * gridDim.x, k = 0, 1, ...
+  for (long long k0 = 0; blockIdx.x + k0 * gridDim.x < nitems; k0 += kMergeThreads) {
+    const long long it = blockIdx.x + (k0 + threadIdx.x) * gridDim.x;
+    const int act = it < nitems && chunk_np[it / kMergeSub] > p;
+    int nact;
+    const int ex = block_exclusive_scan<kMergeThreads>(act, S.scan, &nact);
+    if (act) S.items[ex] = (int)it;
+    __syncthreads();
+    for (int a = 0; a < nact; ++a) {
+      const int item = S.items[a];
+      const int q = item / kMergeSub;
       const int idx = chunk_row[q];
       const int c = long_list[2 * idx];
-      const int L = eoff[c + 1] - eoff[c];
-      // A row is merged in pass p only while it still has more than one run;
-      // rows that finished earlier keep their data in the stage of their parity.
-      if (merge_passes(L) <= p) continue;
-      const int j = q - long_list[2 * idx + 1];
       const long long base = eoff[c];
-      const int o0 = j * kChunk;
+      const int L = eoff[c + 1] - (int)base;
+      const int o0 = (q - long_list[2 * idx + 1]) * kChunk + (item % kMergeSub) * kMergeOut;
+      if (o0 >= L) continue;  // past the end of the row's last (partial) chunk; uniform per block
       const int ps = (int)((o0 / (2 * width)) * (2 * width));
       const int alen = (int)min(width, (long long)(L - ps));
       const int blen = (int)min(width, (long long)(L - ps - alen));
       const int2 *A = src + base + ps;
       const int2 *B = A + alen;
-      const int d0 = o0 - ps, d1 = min(o0 + kChunk, ps + alen + blen) - ps;
+      const int d0 = o0 - ps, d1 = min(o0 + kMergeOut, ps + alen + blen) - ps;
       const int nout = d1 - d0;
-      if (threadIdx.x < 2) {
-        const int d = threadIdx.x == 0 ? d0 : d1;
-        S.cut[threadIdx.x] = blen == 0 ? min(d, alen) : merge_path_g(A, alen, B, blen, d);
+      const int warp = threadIdx.x >> 5;
+      if (warp < 2) {
+        const int d = warp == 0 ? d0 : d1;
+        const int cut = blen == 0 ? min(d, alen) : merge_path_warp(A, alen, B, blen, d);
+        if ((threadIdx.x & 31) == 0) S.cut[warp] = cut;
       }
       __syncthreads();
       const int i0 = S.cut[0], i1 = S.cut[1];
       const int na = i1 - i0, nb = nout - na;
       const int j0 = d0 - i0;
-      for (int t = threadIdx.x; t < na; t += kMergeThreads) S.win[padk<unsigned long long>(t)] = pack_entry(__ldcg(A + i0 + t));
-      for (int t = threadIdx.x; t < nb; t += kMergeThreads)
-        S.win[padk<unsigned long long>(na + t)] = pack_entry(__ldcg(B + j0 + t));
+      // window: A[i0 .. i1) then B[j0 .. j0 + nb)
+      {
+        int2 e[kMergePer];
+#pragma unroll
+        for (int u = 0; u < kMergePer; ++u) {
+          const int t = threadIdx.x + u * kMergeThreads;
+          e[u] = t < na ? __ldcg(A + i0 + t) : (t < nout ? __ldcg(B + j0 + (t - na)) : make_int2(0, 0));
+        }
+#pragma unroll
+        for (int u = 0; u < kMergePer; ++u) {
+          const int t = threadIdx.x + u * kMergeThreads;
+          if (t < nout) S.win[padk<unsigned long long>(t)] = pack_entry(e[u]);
+        }
+      }
       __syncthreads();
       const int od = threadIdx.x * kMergePer;
-      if (od < nout) {
+      const int cnt = max(0, min(kMergePer, nout - od));
+      unsigned long long out[kMergePer];
+      if (cnt > 0) {
         int lo = od > nb ? od - nb : 0, hi = od < na ? od : na;
         while (lo < hi) {
           const int mid = (lo + hi) >> 1;
@@ -637,17 +708,23 @@ k_long_merge(int p, const int *__restrict__ long_list, const int *__restrict__ c
         const unsigned long long kMax = ~0ull;
         unsigned long long ka = ia < na ? S.win[padk<unsigned long long>(ia)] : kMax;
         unsigned long long kb = ib < nb ? S.win[padk<unsigned long long>(na + ib)] : kMax;
-        const int cnt = min(kMergePer, nout - od);
-        for (int t = 0; t < cnt; ++t) {
+#pragma unroll
+        for (int t = 0; t < kMergePer; ++t) {
           const bool takeA = (ib >= nb) || (ia < na && ka <= kb);
-          S.out[padk<unsigned long long>(od + t)] = takeA ? ka : kb;
-          if (takeA) { ++ia; ka = ia < na ? S.win[padk<unsigned long long>(ia)] : kMax; }
-          else { ++ib; kb = ib < nb ? S.win[padk<unsigned long long>(na + ib)] : kMax; }
+          out[t] = takeA ? ka : kb;
+          if (t + 1 < cnt) {
+            if (takeA) { ++ia; ka = ia < na ? S.win[padk<unsigned long long>(ia)] : kMax; }
+            else { ++ib; kb = ib < nb ? S.win[padk<unsigned long long>(na + ib)] : kMax; }
+          }
         }
       }
       __syncthreads();
+#pragma unroll
+      for (int t = 0; t < kMergePer; ++t)
+        if (t < cnt) S.win[padk<unsigned long long>(od + t)] = out[t];
+      __syncthreads();
       int2 *o = dst + base + ps + d0;
-      for (int t = threadIdx.x; t < nout; t += kMergeThreads) o[t] = unpack_entry(S.out[padk<unsigned long long>(t)]);
+      for (int t = threadIdx.x; t < nout; t += kMergeThreads) o[t] = unpack_entry(S.win[padk<unsigned long long>(t)]);
       __syncthreads();
     }
   }
@@ -659,7 +736,7 @@ k_long_merge(int p, const int *__restrict__ long_list, const int *__restrict__ c
 // chunk) is summed and written, compacted within the chunk, to the other stage
 // at eoff[c] + j*kChunk.  chunk_cnt[q] = the chunk's unique entries, also added
 // to ucount[c].
-constexpr int kDedupThreads = 512;
+constexpr int kDedupThreads = 512, kDedupPer = 4;
 __global__ void __launch_bounds__(kDedupThreads)
 k_long_dedup(const int *__restrict__ long_list, const int *__restrict__ chunk_row, const int *__restrict__ eoff,
              const unsigned long long *long_ctr, const int2 *stage0, const int2 *stage1, int2 *out0, int2 *out1,
@@ -676,20 +753,38 @@ k_long_dedup(const int *__restrict__ long_list, const int *__restrict__ chunk_ro
     int2 *dst = (fb ? out0 : out1) + eoff[c] + (long long)j * kChunk;
     const int lo = j * kChunk, hi = min(L, lo + kChunk);
     int carry = 0;
-    for (int b = lo; b < hi; b += kDedupThreads) {
-      const int i = b + threadIdx.x;
-      int h = 0;
-      int2 e = make_int2(0, 0);
-      if (i < hi) {
-        e = src[i];
-        h = ((unsigned)e.x < kPadId) && (i == 0 || src[i - 1].x != e.x);
+    // Each thread takes kDedupPer consecutive entries (loaded together with
+    // the entry before them); a head's run is summed from the thread's own
+    // entries and, past them, from global memory.
+    for (int b = lo; b < hi; b += kDedupThreads * kDedupPer) {
+      const int i0 = b + threadIdx.x * kDedupPer;
+      int2 e[kDedupPer];
+      const int prev = i0 > 0 && i0 < hi ? src[i0 - 1].x : (int)kPadId;
+#pragma unroll
+      for (int u = 0; u < kDedupPer; ++u) e[u] = i0 + u < L ? src[i0 + u] : make_int2((int)kPadId, 0);  // runs may cross hi
+      bool h[kDedupPer];
+      int nh = 0;
+#pragma unroll
+      for (int u = 0; u < kDedupPer; ++u) {
+        const int before = u == 0 ? prev : e[u - 1].x;
+        h[u] = i0 + u < hi && (unsigned)e[u].x < kPadId && (i0 + u == 0 || before != e[u].x);
+        nh += h[u];
       }
       int tot;
-      const int ex = block_exclusive_scan<kDedupThreads>(h, scan, &tot);
-      if (h) {
-        unsigned sum = (unsigned)e.y;
-        for (int k = i + 1; k < L && src[k].x == e.x; ++k) sum += (unsigned)src[k].y;
-        dst[carry + ex] = make_int2(e.x, (int)sum);
+      int o = carry + block_exclusive_scan<kDedupThreads>(nh, scan, &tot);
+#pragma unroll
+      for (int u = 0; u < kDedupPer; ++u) {
+        if (!h[u]) continue;
+        unsigned sum = (unsigned)e[u].y;
+        bool open = true;  // the run still reaches the next entry
+#pragma unroll
+        for (int v = u + 1; v < kDedupPer; ++v) {
+          open = open && e[v].x == e[u].x;
+          if (open) sum += (unsigned)e[v].y;
+        }
+        if (open)
+          for (int k = i0 + kDedupPer; k < L && src[k].x == e[u].x; ++k) sum += (unsigned)src[k].y;
+        dst[o++] = make_int2(e[u].x, (int)sum);
       }
       carry += tot;
     }
@@ -743,10 +838,21 @@ __global__ void k_long_copy(const int *__restrict__ long_list, const int *__rest
       __syncthreads();
       dst = (long long)cxadj[c] + pre;
     }
-    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-      const int2 e = src[t];
-      cadjncy[dst + t] = e.x;
-      cadjwgt[dst + t] = e.y;
+    for (int t0 = threadIdx.x; t0 < cnt; t0 += kCopyBatch * blockDim.x) {
+      int2 e[kCopyBatch];
+#pragma unroll
+      for (int u = 0; u < kCopyBatch; ++u) {
+        const int t = t0 + u * blockDim.x;
+        e[u] = t < cnt ? __ldcs(src + t) : make_int2(0, 0);
+      }
+#pragma unroll
+      for (int u = 0; u < kCopyBatch; ++u) {
+        const int t = t0 + u * blockDim.x;
+        if (t < cnt) {
+          cadjncy[dst + t] = e[u].x;
+          cadjwgt[dst + t] = e[u].y;
+        }
+      }
     }
   }
 }
@@ -765,7 +871,7 @@ size_t contract_ws_bytes(int64_t n, int64_t m) {
   b += (size_t)(ntiles + 2) * 4 + 256;       // first_row
   b += (size_t)(m / kChunk + 2) * 8 + 256;   // long_list
   b += (size_t)(m / (kLongThr + 1) + 2) * 12 + 256;  // size-class lists
-  b += (size_t)nchunks * 4 * 2 + 512;        // chunk_row, chunk_cnt
+  b += (size_t)nchunks * 4 * 3 + 768;        // chunk_row, chunk_cnt, chunk_np
   b += 256;                                  // counters
   b += (size_t)(ntiles + 2) * 8 + 256;       // tile look-back
   b += (size_t)n * 16 + 256;                 // row metadata
@@ -792,13 +898,15 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   int *long_list = (int *)ws_take(ctx, (size_t)(m / kChunk + 2) * 8);
   int *chunk_row = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
   int *chunk_cnt = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
+  int *chunk_np = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
   int *mid_list = (int *)ws_take(ctx, (size_t)mid_cap * 3 * 4);
   int4 *row_meta = (int4 *)ws_take(ctx, (size_t)n * 16);
   unsigned long long *ctr = (unsigned long long *)ws_take(ctx, 64);   // [0] chunked rows, [1] mid counters
   unsigned long long *lb = (unsigned long long *)ws_take(ctx, (size_t)(ntiles + 2) * 8);
   int2 *stage0 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
   int2 *stage1 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
-  if (!leader || !ucount || !eoff || !first_row || !long_list || !chunk_row || !chunk_cnt || !mid_list || !row_meta || !ctr || !lb ||
+  if (!leader || !ucount || !eoff || !first_row || !long_list || !chunk_row || !chunk_cnt || !chunk_np || !mid_list ||
+      !row_meta || !ctr || !lb ||
       !stage0 || !stage1)
     return cm_fail(CM_ERR_NOMEM, "contract: workspace too small");
   int *mid_ctr = reinterpret_cast<int *>(ctr + 1);
@@ -845,16 +953,16 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   // have (m / kChunk), so small graphs do not claim every SM.
   const int long_grid = (int)std::min<int64_t>(sms, m / kChunk / 4 + 1);
   k_long_sort<<<long_grid, kChunkThreads, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
-      fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, long_list, chunk_row, ctr, stage0, ucount);
+      fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, long_list, chunk_row, ctr, stage0, ucount, chunk_np);
   ctx->launches += 4;
   {
     // Passes a row of at most m entries can need; each is a plain launch.
     int max_pass = 0;
     for (int64_t w = kChunk; w < m; w <<= 1) ++max_pass;
-    const int merge_grid = (int)std::min<int64_t>((int64_t)sms * 2, m / kChunk + 1);
+    const int merge_grid = (int)std::min<int64_t>((int64_t)sms * kMergeBlocksPerSm, m / kMergeOut + 1);
     for (int p = 0; p < max_pass; ++p) {
       k_long_merge<<<merge_grid, kMergeThreads, sizeof(MergeSmem), ctx->aux[2]>>>(p, long_list, chunk_row, eoff, ctr,
-                                                                                  stage0, stage1, st);
+                                                                                  chunk_np, stage0, stage1, st);
       ctx->launches++;
     }
   }
