@@ -161,12 +161,13 @@ def _long_row_graph(L_leader, L_follower, extra=0, seed=0):
     return O.CSR(np.cumsum(xadj), dst, w, np.ones(n))
 
 
-@pytest.mark.parametrize("lens", [(512, 512), (512, 513), (1024, 1024), (1024, 1025), (2048, 2048), (2048, 2049),
-                                  (4096, 4096), (4097, 4096), (20000, 13000), (40000, 30000)])
+@pytest.mark.parametrize("lens", [(100, 28), (128, 128), (128, 129), (200, 300), (512, 512), (512, 513), (1024, 1024),
+                                  (1024, 1025), (2048, 2048), (2048, 2049), (4096, 4096), (4097, 4096), (20000, 13000),
+                                  (40000, 30000)])
 def test_long_rows(ctx, lens):
-    """Coarse rows at every path boundary: tile limit 1024, the size classes
-    2048 / 4096 / 8192, and far beyond the 8192-entry chunk (chunk sort,
-    merge passes, dedup, copy)."""
+    """Coarse rows at every path boundary: short rows of a few hundred
+    entries, the tile limit 1024, the size classes 2048 / 4096 / 8192, and far
+    beyond the 8192-entry chunk (chunk sort, merge passes, dedup, copy)."""
     g = _long_row_graph(*lens, extra=500, seed=sum(lens))
     match = np.arange(g.n, dtype=np.int32)
     match[0], match[1] = 1, 0
@@ -188,6 +189,23 @@ def test_many_long_rows(ctx):
     got, gcmap = gpu_contract(ctx, g, match)
     assert np.array_equal(gcmap, wcmap)
     assert_same_graph(got, want, "rmat16")
+
+
+def test_dense_rows_with_weights(ctx):
+    """Rows of about 200 entries everywhere (a geometric graph of mean degree
+    100) with random symmetric weights: tiles of few rows, many duplicates,
+    weights summed."""
+    g = _o(cm.gen_rgg(20000, 100.0, 3))
+    n = g.n
+    src = np.repeat(np.arange(n), np.diff(g.xadj))
+    lo, hi = np.minimum(src, g.adjncy).astype(np.int64), np.maximum(src, g.adjncy).astype(np.int64)
+    w = (1 + (lo * 1000003 + hi * 7919) % 1000).astype(np.int32)
+    g = O.CSR(g.xadj, g.adjncy, w, g.vwgt)
+    match = O.match_greedy(g, O.maxvwgt_rule(int(g.vwgt.sum()), 1000), 1)
+    want, wcmap = O.contract(g, match)
+    got, gcmap = gpu_contract(ctx, g, match)
+    assert np.array_equal(gcmap, wcmap)
+    assert_same_graph(got, want, "rgg deg 100")
 
 
 def test_build_cmap(ctx, graphs):
