@@ -475,7 +475,7 @@ extern "C" int cm_part_graph(cm_ctx *ctx, int32_t nvtxs, const int32_t *xadj, co
                              cm_part_stats *stats) {
   (void)tpwgts;  // accepted and ignored, as by the reference (cu:370-394)
   (void)ubvec;
-  if (!ctx || nvtxs < 0 || !part || nparts < 1 || (nvtxs > 0 && (!xadj || (xadj[nvtxs] > 0 && !adjncy))))
+  if (!ctx || nvtxs < 0 || !part || nparts < 1 || (nvtxs > 0 && (!xadj || xadj[nvtxs] < 0 || (xadj[nvtxs] > 0 && !adjncy))))
     return cm_fail(CM_ERR_INVALID, "cm_part_graph: bad arguments");
   cm_part_params P;
   cm_part_default_params(&P);
@@ -502,7 +502,7 @@ extern "C" int cm_part_graph(cm_ctx *ctx, int32_t nvtxs, const int32_t *xadj, co
     ue.assign(std::max<int64_t>(m, 1), 1);
     adjwgt = ue.data();
   }
-  cm_graph hg{nvtxs, m, const_cast<int32_t *>(xadj), const_cast<int32_t *>(adjncy), const_cast<int32_t *>(adjwgt),
+  cm_graph hg{nvtxs, (int32_t)m, const_cast<int32_t *>(xadj), const_cast<int32_t *>(adjncy), const_cast<int32_t *>(adjwgt),
               const_cast<int32_t *>(vwgt)};
   cm_coarsen_params cp;
   cm_coarsen_default_params(nvtxs, nparts, &cp);
