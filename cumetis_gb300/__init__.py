@@ -13,7 +13,8 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "libcm.so")
+# CUMETIS_LIB selects another build of the library (the autotuner's variants).
+LIB_PATH = os.environ.get("CUMETIS_LIB") or os.path.join(_HERE, "libcm.so")
 CLI_PATH = os.path.join(_HERE, "cuMetis")
 
 CM_OK, CM_ERR_INVALID, CM_ERR_NOMEM, CM_ERR_CUDA, CM_ERR_LIMIT, CM_ERR_IO, CM_ERR_UNSUPPORTED = range(7)

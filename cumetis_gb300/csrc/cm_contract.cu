@@ -43,12 +43,25 @@ constexpr int kTileThreads = CM_TILE_THREADS;     // threads per contraction til
 #endif
 constexpr int kTileE = CM_TILE_E;                 // keys per lane in the tile sort's register runs
 constexpr int kTileDiag = 512;                    // D
-constexpr int kLongThr = 1024;                    // rows longer than this take the long path
+// Rows longer than kLongThr take the long path; rows longer than kChunk are
+// sorted in kChunk-entry chunks and merged.  Both are tuning parameters (the
+// autotuner's choice lands here through the build).
+#ifndef CM_LONG_THR
+#define CM_LONG_THR 1024
+#endif
+#ifndef CM_CHUNK
+#define CM_CHUNK 8192
+#endif
+constexpr int kLongThr = CM_LONG_THR;
 constexpr int kTileCap = kTileDiag + kLongThr;    // max entries in a tile (multiple of kTileE)
-constexpr int kChunk = 8192;                      // long-row chunk (entries sorted per block)
+constexpr int kChunk = CM_CHUNK;                  // long-row chunk (entries sorted per block)
 constexpr int kChunkThreads = 1024;
+static_assert(kLongThr == 512 || kLongThr == 1024 || kLongThr == 2048, "CM_LONG_THR: 512, 1024 or 2048");
+static_assert(kChunk == 4096 || kChunk == 8192, "CM_CHUNK: 4096 or 8192 (one block's shared memory)");
+static_assert(4 * kLongThr <= kChunk, "the size classes 2x and 4x CM_LONG_THR must fit a chunk");
 // Threads per block of the three size classes of rows between kLongThr and
-// kChunk entries (1025-2048, 2049-4096, 4097-8192).
+// kChunk entries ((T, 2T], (2T, 4T], (4T, kChunk] for T = kLongThr; with the
+// defaults 1025-2048, 2049-4096, 4097-8192).
 #ifndef CM_MID_THREADS0
 #define CM_MID_THREADS0 256
 #endif
@@ -165,7 +178,8 @@ __device__ __forceinline__ int hash_compact(const K *hk, int hsize, K *dst, int 
 // ---------------------------------------------------------------------------
 // Contraction tiles
 // ---------------------------------------------------------------------------
-constexpr int kTileHashLog2 = 11;                 // 2048 slots (> kTileCap, load <= 3/4)
+__host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v >> 1); }
+constexpr int kTileHashLog2 = ilog2(kTileCap) + 1;  // the power of two above kTileCap (2048 for 1536)
 constexpr int kTileHash = 1 << kTileHashLog2;
 static_assert(kTileHash > kTileCap, "tile hash must have a free slot for every entry");
 
@@ -477,8 +491,6 @@ struct MidSmem {
   int hw[2 * CAP];
   int ctr;
 };
-
-__host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v >> 1); }
 
 // Gathers entries [cs, cs + cnt) of coarse row c's expanded row (metadata
 // md), merges duplicates in a shared-memory hash set that sums the weights

@@ -46,8 +46,18 @@ namespace {
 #endif
 constexpr int kMatchThreads = CM_MATCH_THREADS, kMatchMinBlocks = CM_MATCH_MINBLOCKS;
 constexpr int64_t kWorkPerBlock = 32768;  // vertices + entries per block of the matching grid
-constexpr int kSerialDeg = 16;   // rows scanned by one lane
-constexpr int kChunk = 256;      // entries per warp work item
+// Rows of at most kSerialDeg entries are scanned by one lane, longer rows in
+// kChunk-entry warp work items (tuning parameters, set through the build).
+#ifndef CM_SERIAL_DEG
+#define CM_SERIAL_DEG 16
+#endif
+#ifndef CM_MATCH_CHUNK
+#define CM_MATCH_CHUNK 256
+#endif
+constexpr int kSerialDeg = CM_SERIAL_DEG;
+constexpr int kChunk = CM_MATCH_CHUNK;
+static_assert(kSerialDeg == 8 || kSerialDeg == 16, "CM_SERIAL_DEG: 8 or 16");
+static_assert(kChunk == 128 || kChunk == 256 || kChunk == 512, "CM_MATCH_CHUNK: 128, 256 or 512");
 constexpr int kTop = 4;          // cached candidates per vertex
 constexpr int kNotScanned = -2;  // top[v*kTop] before the first scan
 constexpr int kUnknown = -3;     // cache slot not computed (the first scan keeps only the best)
