@@ -208,6 +208,44 @@ def test_dense_rows_with_weights(ctx):
     assert_same_graph(got, want, "rgg deg 100")
 
 
+def _messy_graph(n=4000, seed=7):
+    """A symmetric multigraph the reference's kernels accept but METIS files
+    never hold: self loops, parallel edges (each with its own weight), rows in
+    random order, and weights of 0, negative and near INT_MAX, so that
+    merged weights wrap around int32."""
+    rng = np.random.default_rng(seed)
+    m = 6 * n
+    a, b = rng.integers(0, n, m), rng.integers(0, n, m)
+    par = rng.choice(m, m // 8)                                   # parallel copies of 1/8 of the edges
+    loops = rng.choice(n, 60, replace=False)                      # explicit self loops
+    a, b = np.r_[a, a[par], loops], np.r_[b, b[par], loops]
+    w = rng.choice(np.array([0, 1, 3, 17, -5, 1 << 30, (1 << 31) - 1], np.int64), len(a),
+                   p=[0.05, 0.4, 0.2, 0.15, 0.05, 0.1, 0.05])
+    src = np.r_[a, b[a != b]]
+    dst = np.r_[b, a[a != b]]
+    ww = np.r_[w, w[a != b]]
+    order = np.lexsort((rng.random(len(src)), src))              # grouped by row, random order within
+    src, dst, ww = src[order], dst[order], ww[order]
+    xadj = np.zeros(n + 1, np.int64)
+    np.add.at(xadj, src + 1, 1)
+    return O.CSR(np.cumsum(xadj), dst, ww.astype(np.int32), 1 + (np.arange(n) % 3))
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_messy_input_bitexact(ctx, mode):
+    """Self loops, parallel edges, unsorted rows, extreme and wrapping
+    weights: matching and contraction still bit-exact against the oracle."""
+    g = _messy_graph()
+    mv = O.maxvwgt_rule(int(g.vwgt.sum()), 300)
+    want = O.match_greedy(g, mv, mode)
+    got, _ = gpu_match(ctx, g, mv, mode)
+    assert np.array_equal(got, want)
+    wcg, wcmap = O.contract(g, want)
+    cg, gcmap = gpu_contract(ctx, g, want)
+    assert np.array_equal(gcmap, wcmap)
+    assert_same_graph(cg, wcg, "messy")
+
+
 def test_build_cmap(ctx, graphs):
     import torch
     for name, g in graphs.items():
