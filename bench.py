@@ -372,7 +372,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="rmat22", choices=sorted(WORKLOADS) + ["batch", "serve"])
-    ap.add_argument("--workers", type=int, default=8, help="batch/serve: worker threads (one context each)")
+    ap.add_argument("--workers", type=int, default=16, help="batch/serve: worker threads (one context each)")
     ap.add_argument("--batch-graphs", type=int, default=4096)
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: offered requests/s")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: arrival window in seconds")
