@@ -4,8 +4,8 @@
 
 Each tuning parameter is a macro of one CUDA source (the warp-per-vertex
 threshold and the warp work-item size of the matching, the tile / long-row
-threshold and the chunk size of the contraction, the block shapes of their
-kernels).  The search is coordinate descent from the current tuning file (or
+threshold, the tile size and the chunk size of the contraction, the block
+shapes of their kernels).  The search is coordinate descent from the current tuning file (or
 the compiled-in defaults): for each parameter in turn every other candidate
 value is built as a library variant (only the source it belongs to is
 recompiled), timed with bench.py in a fresh process on the same workload,
@@ -32,6 +32,7 @@ PARAMS = [
     ("CM_FIRST_KEEP_SHORT", 2, [1, 2, 4], "cm_match.cu"),    # candidates the first round keeps
     ("CM_LONG_THR", 1024, [512, 1024, 2048], "cm_contract.cu"),  # tile / long-row threshold
     ("CM_CHUNK", 8192, [4096, 8192], "cm_contract.cu"),      # long-row segment (chunk) size
+    ("CM_TILE_DIAG", 512, [511, 512, 1023], "cm_contract.cu"),  # tile size (rows + entries)
     ("CM_TILE_THREADS", 256, [128, 256], "cm_contract.cu"),
     ("CM_MID_THREADS0", 256, [128, 256, 512], "cm_contract.cu"),
     ("CM_MID_THREADS1", 512, [256, 512, 1024], "cm_contract.cu"),

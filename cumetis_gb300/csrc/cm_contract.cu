@@ -42,7 +42,12 @@ constexpr int kTileThreads = CM_TILE_THREADS;     // threads per contraction til
 #define CM_TILE_E 4
 #endif
 constexpr int kTileE = CM_TILE_E;                 // keys per lane in the tile sort's register runs
-constexpr int kTileDiag = 512;                    // D
+// D, diagonals per tile (a tuning parameter).  A tile holds at most D rows,
+// so its row index needs kTileRowBits bits.
+#ifndef CM_TILE_DIAG
+#define CM_TILE_DIAG 512
+#endif
+constexpr int kTileDiag = CM_TILE_DIAG;
 // Rows longer than kLongThr take the long path; rows longer than kChunk are
 // sorted in kChunk-entry chunks and merged.  Both are tuning parameters (the
 // autotuner's choice lands here through the build).
@@ -53,7 +58,7 @@ constexpr int kTileDiag = 512;                    // D
 #define CM_CHUNK 8192
 #endif
 constexpr int kLongThr = CM_LONG_THR;
-constexpr int kTileCap = kTileDiag + kLongThr;    // max entries in a tile (multiple of kTileE)
+constexpr int kTileCap = kTileDiag + kLongThr;    // a tile holds fewer entries than this
 constexpr int kChunk = CM_CHUNK;                  // long-row chunk (entries sorted per block)
 constexpr int kChunkThreads = 1024;
 static_assert(kLongThr == 512 || kLongThr == 1024 || kLongThr == 2048, "CM_LONG_THR: 512, 1024 or 2048");
@@ -70,13 +75,21 @@ static_assert(4 * kLongThr <= kChunk, "the size classes 2x and 4x CM_LONG_THR mu
 #endif
 constexpr int kMidThreads0 = CM_MID_THREADS0, kMidThreads1 = CM_MID_THREADS1;
 
-// Composite key (tile-local row, coarse id).  32-bit when coarse ids fit in
-// 23 bits (n < 2^23 - 1; rows need 9 bits for kTileDiag = 512), else 64-bit.
-// All-ones is the empty hash slot and the sort pad; no key reaches it.
+// Composite key (tile-local row, coarse id).  32-bit when the coarse ids fit
+// the bits the row index leaves (kTileIdBits), else 64-bit.  All-ones is the
+// empty hash slot and the sort pad; no key reaches it: with D < 2^rowbits the
+// row field never reaches all-ones, with D = 2^rowbits the id field must not
+// (n < 2^idbits).
+__host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v >> 1); }
+constexpr int kTileRowBits = ilog2(kTileDiag - 1) + 1;  // rows 0 .. D-1
+constexpr int kTileIdBits = 32 - kTileRowBits;
+constexpr long long kSmallIdMaxN =                       // largest n with 32-bit keys
+    kTileDiag < (1 << kTileRowBits) ? (1ll << kTileIdBits) : (1ll << kTileIdBits) - 1;
+static_assert(kTileDiag >= 256 && kTileDiag <= 1024, "CM_TILE_DIAG: 256 .. 1024");
 template <typename K> struct KeyT;
 template <> struct KeyT<unsigned> {
-  static constexpr int kShift = 23;
-  static constexpr unsigned kIdMask = (1u << 23) - 1;
+  static constexpr int kShift = kTileIdBits;
+  static constexpr unsigned kIdMask = (1u << kTileIdBits) - 1;
   static __device__ __forceinline__ unsigned make(int r, unsigned id) { return ((unsigned)r << kShift) | id; }
   static __device__ __forceinline__ int row(unsigned k) { return (int)(k >> kShift); }
   static __device__ __forceinline__ unsigned id(unsigned k) { return k & kIdMask; }
@@ -88,8 +101,6 @@ template <> struct KeyT<unsigned long long> {
   static __device__ __forceinline__ int row(unsigned long long k) { return (int)(k >> 32); }
   static __device__ __forceinline__ unsigned id(unsigned long long k) { return (unsigned)k; }
 };
-constexpr int kSmallIdLimit = (1 << 23) - 1;   // n below this uses 32-bit keys
-static_assert(kTileDiag <= 512, "tile rows must fit in 9 bits");
 
 __device__ __forceinline__ int upper_bound_smem(const int *a, int n, int x) {
   int lo = 0, hi = n;
@@ -178,8 +189,9 @@ __device__ __forceinline__ int hash_compact(const K *hk, int hsize, K *dst, int 
 // ---------------------------------------------------------------------------
 // Contraction tiles
 // ---------------------------------------------------------------------------
-__host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v >> 1); }
-constexpr int kTileHashLog2 = ilog2(kTileCap) + 1;  // the power of two above kTileCap (2048 for 1536)
+// Table slots: the power of two of at least 4/3 kTileCap (load <= 3/4; 2048
+// for the default kTileCap of 1536).
+constexpr int kTileHashLog2 = ilog2((4 * kTileCap + 2) / 3 - 1) + 1;
 constexpr int kTileHash = 1 << kTileHashLog2;
 static_assert(kTileHash > kTileCap, "tile hash must have a free slot for every entry");
 
@@ -191,7 +203,7 @@ template <typename K>
 struct TileSmem {
   union {
     TileRows T;                                   // gather
-    K keys[2][padded_k<K>(kTileCap + 8)];         // sort of the unique keys
+    K keys[2][padded_k<K>(((kTileCap + 32 * kTileE - 1) / (32 * kTileE)) * 32 * kTileE)];  // sort of the unique keys
   } u;
   K hk[kTileHash];
   int hw[kTileHash];
@@ -218,7 +230,7 @@ __device__ __forceinline__ int tile_rows(TileSmem<K> &S, int tile, int nc, long 
     R = 0;
   }
   if (R == 0) return 0;  // a tile inside a long row's diagonal span holds no row
-  constexpr int kRowsPerThread = kTileDiag / kTileThreads;
+  constexpr int kRowsPerThread = (kTileDiag + kTileThreads - 1) / kTileThreads;
   int lens[kRowsPerThread];
   int mysum = 0;
 #pragma unroll
@@ -412,7 +424,7 @@ k_copy_tiles(const int *__restrict__ eoff, const int *d_cn, const int *__restric
   const int chi = t1 <= last ? first_row[t1] : nc;
   const int R = max(0, min(kCopyRows, chi - clo));
   if (R == 0) return;  // tiles inside a long row's diagonal span
-  constexpr int kRowsPerThread = kCopyRows / kCopyThreads;
+  constexpr int kRowsPerThread = (kCopyRows + kCopyThreads - 1) / kCopyThreads;
   int cnt[kRowsPerThread];
   int mysum = 0;
 #pragma unroll
@@ -931,7 +943,7 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
                        kTileDiag, mid_list, mid_ctr, (int32_t)mid_cap, row_meta, s);
   if (rc) return rc;
   const int sms = ctx->num_sms;
-  const bool small_ids = n < kSmallIdLimit;
+  const bool small_ids = n <= kSmallIdMaxN;
   const size_t tile_smem = small_ids ? sizeof(TileSmem<unsigned>) : sizeof(TileSmem<unsigned long long>);
   if (small_ids)
     cudaFuncSetAttribute(k_contract_tiles<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem);
