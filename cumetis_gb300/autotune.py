@@ -29,11 +29,13 @@ PARAMS = [
     ("CM_SERIAL_DEG", 16, [8, 16], "cm_match.cu"),          # rows scanned by one lane (warp-per-vertex threshold)
     ("CM_MATCH_CHUNK", 256, [128, 256, 512], "cm_match.cu"),  # entries per warp work item
     ("CM_FIRST_MINBLOCKS", 8, [4, 6, 8], "cm_match.cu"),     # first-round kernel: blocks per SM (register cap)
-    ("CM_FIRST_KEEP_SHORT", 2, [1, 2, 4], "cm_match.cu"),    # candidates the first round keeps
+    ("CM_FIRST_KEEP_SHORT", 2, [1, 2, 4], "cm_match.cu"),    # candidates the first round keeps (lane rows)
+    ("CM_FIRST_KEEP_CHUNK", 2, [1, 2, 4], "cm_match.cu"),    # ... and per chunked row
     ("CM_LONG_THR", 1024, [512, 1024, 2048], "cm_contract.cu"),  # tile / long-row threshold
     ("CM_CHUNK", 8192, [4096, 8192], "cm_contract.cu"),      # long-row segment (chunk) size
     ("CM_TILE_DIAG", 512, [511, 512, 1023], "cm_contract.cu"),  # tile size (rows + entries)
     ("CM_TILE_THREADS", 256, [128, 256], "cm_contract.cu"),
+    ("CM_TILE_E", 4, [2, 4, 8], "cm_contract.cu"),           # keys per lane of the tile sort's warp runs
     ("CM_MID_THREADS0", 256, [128, 256, 512], "cm_contract.cu"),
     ("CM_MID_THREADS1", 512, [256, 512, 1024], "cm_contract.cu"),
     ("CM_MERGE_THREADS", 256, [256, 512], "cm_contract.cu"),
