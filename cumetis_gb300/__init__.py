@@ -120,6 +120,7 @@ def _declare(L):
         "cm_ctx_stage_times": (c_int, [c_vp, ctypes.POINTER(ctypes.c_double), c_i32, c_int]),
         "cm_stage_name": (ctypes.c_char_p, [c_i32]),
         "cm_ctx_set_match_trace": (c_int, [c_vp, c_i32]),
+        "cm_ctx_set_blocking_waits": (c_int, [c_vp, c_int]),
         "cm_ctx_match_trace": (c_int, [c_vp, ctypes.POINTER(ctypes.c_int64), c_i32, _I32P]),
         "cm_hierarchy_read_level": (c_int, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp]),
         "cm_refine_kway": (c_int, [c_vp, G, c_i32, c_vp, ctypes.POINTER(c_i64), c_vp]),

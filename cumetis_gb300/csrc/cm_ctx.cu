@@ -91,12 +91,18 @@ void stage_end(cm_ctx *ctx, int stage, cudaStream_t s) {
 
 int set_device(cm_ctx *ctx) { return cuda_status(cudaSetDevice(ctx->device), "cudaSetDevice"); }
 
+int stream_wait(cm_ctx *ctx, cudaStream_t s, const char *what) {
+  if (!ctx->blocking_waits || !ctx->wait_ev) return cuda_status(cudaStreamSynchronize(s), what);
+  int rc = cuda_status(cudaEventRecord(ctx->wait_ev, s), what);
+  return rc ? rc : cuda_status(cudaEventSynchronize(ctx->wait_ev), what);
+}
+
 // Reads the device status, clears its error, returns it as a CM status.
 int take_device_error(cm_ctx *ctx, cudaStream_t s) {
   int rc = cuda_status(cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s),
                        "status readback");
   if (rc) return rc;
-  rc = cuda_status(cudaStreamSynchronize(s), "stream sync");
+  rc = stream_wait(ctx, s, "stream sync");
   if (rc) return rc;
   const int err = ctx->h_status->error, site = ctx->h_status->error_site;
   if (err) {
@@ -174,6 +180,9 @@ extern "C" int cm_ctx_create(int device, cm_ctx **out) {
     if (!rc) rc = cuda_status(cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming), "aux event");
   }
   if (!rc) rc = cuda_status(cudaEventCreateWithFlags(&ctx->fork_ev, cudaEventDisableTiming), "fork event");
+  if (!rc)
+    rc = cuda_status(cudaEventCreateWithFlags(&ctx->wait_ev, cudaEventDisableTiming | cudaEventBlockingSync),
+                     "wait event");
   if (!rc) {
     // The context's own pool; freed level buffers stay in it between calls.
     cudaMemPoolProps props = {};
@@ -211,6 +220,7 @@ extern "C" void cm_ctx_destroy(cm_ctx *ctx) {
     if (ctx->join_ev[i]) cudaEventDestroy(ctx->join_ev[i]);
   }
   if (ctx->fork_ev) cudaEventDestroy(ctx->fork_ev);
+  if (ctx->wait_ev) cudaEventDestroy(ctx->wait_ev);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->pool) cudaMemPoolDestroy(ctx->pool);  // blocks still held by hierarchies keep it alive until freed
   delete ctx;
@@ -245,6 +255,12 @@ extern "C" int64_t cm_ctx_launch_count(const cm_ctx *ctx) { return ctx ? ctx->la
 extern "C" int cm_ctx_set_stage_timing(cm_ctx *ctx, int enable) {
   if (!ctx) return cm_fail(CM_ERR_INVALID, "cm_ctx_set_stage_timing: null context");
   ctx->timing = enable != 0;
+  return CM_OK;
+}
+
+extern "C" int cm_ctx_set_blocking_waits(cm_ctx *ctx, int enable) {
+  if (!ctx) return cm_fail(CM_ERR_INVALID, "cm_ctx_set_blocking_waits: null context");
+  ctx->blocking_waits = enable != 0;
   return CM_OK;
 }
 
@@ -447,7 +463,7 @@ extern "C" int cm_coarsen(cm_ctx *ctx, const cm_graph *g, int input_on_device, c
     ctx->launches++;
     unsigned long long hs = 0;
     if ((rc = cuda_status(cudaMemcpyAsync(&hs, d_sum, 8, cudaMemcpyDeviceToHost, s), "tvwgt readback")) ||
-        (rc = cuda_status(cudaStreamSynchronize(s), "tvwgt sync")))
+        (rc = stream_wait(ctx, s, "tvwgt sync")))
       return fail(rc);
     tvwgt = (int64_t)hs;
   } else {
@@ -486,7 +502,7 @@ extern "C" int cm_coarsen(cm_ctx *ctx, const cm_graph *g, int input_on_device, c
     cudaMemcpyAsync(ctx->h_status, ctx->d_status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
     int32_t *hsz = ctx->h_small;
     cudaMemcpyAsync(hsz, sizes, 8, cudaMemcpyDeviceToHost, s);
-    if ((rc = cuda_status(cudaStreamSynchronize(s), "level sync"))) { cudaFreeAsync(C.block, s); return fail(rc); }
+    if ((rc = stream_wait(ctx, s, "level sync"))) { cudaFreeAsync(C.block, s); return fail(rc); }
     if (ctx->h_status->error) {
       cudaFreeAsync(C.block, s);
       rc = take_device_error(ctx, s);  // also resets the status block

@@ -40,6 +40,10 @@ struct cm_ctx {
   // matching trace (optional): 8 x uint64 per row, row 0 = header
   unsigned long long *d_trace = nullptr;
   int trace_rows = 0;
+  // host waits: spin (default) or sleep on a blocking-sync event, which
+  // frees the core for other host work (the engine's workers)
+  bool blocking_waits = false;
+  cudaEvent_t wait_ev = nullptr;
 };
 
 namespace cm {
@@ -58,6 +62,9 @@ void stage_end(cm_ctx *ctx, int stage, cudaStream_t s);
 
 // Makes the context's device current.
 int set_device(cm_ctx *ctx);
+// Waits until the work queued on s so far is done: a stream synchronisation,
+// or with ctx->blocking_waits a blocking-sync event (the thread sleeps).
+int stream_wait(cm_ctx *ctx, cudaStream_t s, const char *what);
 // Reads the device status block on stream s, clears a recorded error and
 // returns it as a CM status (CM_OK when none).
 int take_device_error(cm_ctx *ctx, cudaStream_t s);

@@ -408,7 +408,7 @@ int edge_cut_dev(cm_ctx *ctx, const cm_graph &g, const int32_t *where, unsigned 
   ctx->launches++;
   unsigned long long h = 0;
   int rc = cuda_status(cudaMemcpyAsync(&h, d_out, 8, cudaMemcpyDeviceToHost, s), "cut readback");
-  if (!rc) rc = cuda_status(cudaStreamSynchronize(s), "cut sync");
+  if (!rc) rc = stream_wait(ctx, s, "cut sync");
   if (!rc) *cut = (int64_t)(h / 2);
   return rc;
 }
@@ -439,7 +439,7 @@ extern "C" int cm_refine_kway(cm_ctx *ctx, const cm_graph *g_dev, int32_t nparts
   if (moves) {
     unsigned long long h = 0;
     if ((rc = cuda_status(cudaMemcpyAsync(&h, w.counters, 8, cudaMemcpyDeviceToHost, s), "moves readback")) ||
-        (rc = cuda_status(cudaStreamSynchronize(s), "moves sync")))
+        (rc = stream_wait(ctx, s, "moves sync")))
       return rc;
     *moves = (int64_t)h;
   }
@@ -556,7 +556,7 @@ extern "C" int cm_part_graph(cm_ctx *ctx, int32_t nvtxs, const int32_t *xadj, co
   }
   auto finish = [&](int code) {
     cudaFreeAsync(wbuf, s);
-    cudaStreamSynchronize(s);
+    stream_wait(ctx, s, "free");
     cm_hierarchy_free(h);
     return code;
   };
@@ -582,7 +582,7 @@ extern "C" int cm_part_graph(cm_ctx *ctx, int32_t nvtxs, const int32_t *xadj, co
   cudaMemcpyAsync(&moves, w.counters, 8, cudaMemcpyDeviceToHost, s);
   if ((rc = cuda_status(cudaMemcpyAsync(part, wl[0], (size_t)nvtxs * 4, cudaMemcpyDeviceToHost, s), "part readback")))
     return finish(rc);
-  if ((rc = cuda_status(cudaStreamSynchronize(s), "part sync"))) return finish(rc);
+  if ((rc = stream_wait(ctx, s, "part sync"))) return finish(rc);
   S.uncoarsen_ms = ms_since(t0);
   S.moves = (int64_t)moves;
   S.edge_cut = cut;

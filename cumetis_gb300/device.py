@@ -75,6 +75,10 @@ class Context:
         _check(lib().cm_ctx_stage_times(self._h, buf, n, 1 if reset else 0))
         return {lib().cm_stage_name(i).decode(): float(buf[i]) for i in range(n)}
 
+    def set_blocking_waits(self, enable=True):
+        """Sleep instead of spinning while the library waits on the GPU."""
+        _check(lib().cm_ctx_set_blocking_waits(self._h, 1 if enable else 0))
+
     def set_match_trace(self, max_rounds):
         _check(lib().cm_ctx_set_match_trace(self._h, int(max_rounds)))
 

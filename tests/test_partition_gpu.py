@@ -124,6 +124,26 @@ def test_part_graph_two_parts_matches_pipeline_model(ctx, name):
     assert st["edge_cut"] == cut and st["levels"] >= 2
 
 
+def test_blocking_waits_same_result():
+    """A context that sleeps on blocking-sync events while the GPU works (the
+    engine workers' setting) gives the same two-part partition as a spinning
+    one, through the whole pipeline."""
+    g = GRAPHS["rmat11"]()
+    a, b = cm.Context(0), cm.Context(0)
+    try:
+        b.set_blocking_waits(True)
+        pa, ca, _ = a.part_graph(g, 2, seed=3)
+        pb, cb, _ = b.part_graph(g, 2, seed=3)
+        np.testing.assert_array_equal(pa, pb)
+        assert ca == cb
+        h = b.coarsen(g, cm.coarsen_threshold(g.nvtxs, 8))
+        assert len(h) >= 2
+        h.close()
+    finally:
+        a.close()
+        b.close()
+
+
 @pytest.mark.parametrize("k", [4, 8, 64])
 def test_part_graph_kway_quality(ctx, k):
     g = cm.gen_grid2d(200, 150)
