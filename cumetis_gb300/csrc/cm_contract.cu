@@ -905,7 +905,7 @@ size_t contract_ws_bytes(int64_t n, int64_t m) {
 }
 
 int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int32_t *cmap, cm_graph *coarse,
-                    int32_t *d_sizes, cudaStream_t s) {
+                    int32_t *d_sizes, cudaStream_t s, int64_t row_bound) {
   const int64_t n = fine->nvtxs, m = fine->nedges;
   if (n == 0) {
     cudaMemsetAsync(d_sizes, 0, 2 * sizeof(int32_t), s);
@@ -963,37 +963,53 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   // rows' sort, merge passes and dedup after the largest class) while the
   // tiles do the short rows on the caller's stream.  All of them leave their
   // unique entries in stage1 at eoff[c] (the chunked rows in the stage their
-  // merge parity picks) and their number in ucount[c].
+  // merge parity picks) and their number in ucount[c].  Classes above
+  // row_bound (an upper bound of the expanded row length known to the
+  // caller) cannot have rows and are not launched.
+  const bool any_long = row_bound > kLongThr;
+  const bool class1 = row_bound > 2 * kLongThr, class2 = row_bound > 4 * kLongThr, chunked = row_bound > kChunk;
   stage_begin(ctx, s);
-  cudaEventRecord(ctx->fork_ev, s);
-  for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(ctx->aux[i], ctx->fork_ev, 0);
-  k_mid_rows<kMidThreads0, 2 * kLongThr><<<grid_for(sms * 4, m / (kLongThr + 1)), kMidThreads0, sizeof(MidSmem<2 * kLongThr>), ctx->aux[0]>>>(
-      fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list, mid_ctr + 0, stage1, ucount);
-  k_mid_rows<kMidThreads1, 4 * kLongThr><<<grid_for(sms * 2, m / (2 * kLongThr + 1)), kMidThreads1, sizeof(MidSmem<4 * kLongThr>), ctx->aux[1]>>>(
-      fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + mid_cap, mid_ctr + 1, stage1, ucount);
-  k_mid_rows<1024, kChunk><<<grid_for(sms, m / (4 * kLongThr + 1)), 1024, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
-      fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + 2 * mid_cap, mid_ctr + 2, stage1, ucount);
-  // Grids of the chunked-row kernels scale with the most chunks the graph can
-  // have (m / kChunk), so small graphs do not claim every SM.
-  const int long_grid = (int)std::min<int64_t>(sms, m / kChunk / 4 + 1);
-  k_long_sort<<<long_grid, kChunkThreads, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
-      fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, long_list, chunk_row, ctr, stage0, ucount, chunk_np);
-  ctx->launches += 4;
-  {
-    // Passes a row of at most m entries can need; each is a plain launch.
-    int max_pass = 0;
-    for (int64_t w = kChunk; w < m; w <<= 1) ++max_pass;
-    const int merge_grid = (int)std::min<int64_t>((int64_t)sms * kMergeBlocksPerSm, m / kMergeOut + 1);
-    for (int p = 0; p < max_pass; ++p) {
-      k_long_merge<<<merge_grid, kMergeThreads, sizeof(MergeSmem), ctx->aux[2]>>>(p, long_list, chunk_row, eoff, ctr,
-                                                                                  chunk_np, stage0, stage1, st);
+  if (any_long) {
+    cudaEventRecord(ctx->fork_ev, s);
+    for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(ctx->aux[i], ctx->fork_ev, 0);
+    k_mid_rows<kMidThreads0, 2 * kLongThr><<<grid_for(sms * 4, m / (kLongThr + 1)), kMidThreads0,
+                                             sizeof(MidSmem<2 * kLongThr>), ctx->aux[0]>>>(
+        fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list, mid_ctr + 0, stage1, ucount);
+    ctx->launches++;
+    if (class1) {
+      k_mid_rows<kMidThreads1, 4 * kLongThr><<<grid_for(sms * 2, m / (2 * kLongThr + 1)), kMidThreads1,
+                                               sizeof(MidSmem<4 * kLongThr>), ctx->aux[1]>>>(
+          fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + mid_cap, mid_ctr + 1, stage1, ucount);
       ctx->launches++;
     }
+    if (class2) {
+      k_mid_rows<1024, kChunk><<<grid_for(sms, m / (4 * kLongThr + 1)), 1024, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
+          fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + 2 * mid_cap, mid_ctr + 2, stage1, ucount);
+      ctx->launches++;
+    }
+    if (chunked) {
+      // Grids of the chunked-row kernels scale with the most chunks the graph
+      // can have (m / kChunk), so small graphs do not claim every SM.
+      const int long_grid = (int)std::min<int64_t>(sms, m / kChunk / 4 + 1);
+      k_long_sort<<<long_grid, kChunkThreads, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
+          fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, long_list, chunk_row, ctr, stage0, ucount, chunk_np);
+      ctx->launches++;
+      // Passes a row of at most min(m, row_bound) entries can need; each is a
+      // plain launch.
+      int max_pass = 0;
+      for (int64_t w = kChunk; w < std::min<int64_t>(m, row_bound); w <<= 1) ++max_pass;
+      const int merge_grid = (int)std::min<int64_t>((int64_t)sms * kMergeBlocksPerSm, m / kMergeOut + 1);
+      for (int p = 0; p < max_pass; ++p) {
+        k_long_merge<<<merge_grid, kMergeThreads, sizeof(MergeSmem), ctx->aux[2]>>>(p, long_list, chunk_row, eoff, ctr,
+                                                                                    chunk_np, stage0, stage1, st);
+        ctx->launches++;
+      }
+      k_long_dedup<<<long_grid * 4, kDedupThreads, 0, ctx->aux[2]>>>(long_list, chunk_row, eoff, ctr, stage0, stage1,
+                                                                     stage0, stage1, chunk_cnt, ucount);
+      ctx->launches++;
+    }
+    for (int i = 0; i < 3; ++i) cudaEventRecord(ctx->join_ev[i], ctx->aux[i]);
   }
-  k_long_dedup<<<long_grid * 4, kDedupThreads, 0, ctx->aux[2]>>>(long_list, chunk_row, eoff, ctr, stage0, stage1, stage0,
-                                                            stage1, chunk_cnt, ucount);
-  ctx->launches++;
-  for (int i = 0; i < 3; ++i) cudaEventRecord(ctx->join_ev[i], ctx->aux[i]);
   // d_sizes[0] holds n' (written by the cmap scan).
   if (small_ids)
     k_contract_tiles<unsigned><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
@@ -1002,7 +1018,8 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
     k_contract_tiles<unsigned long long><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
         fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, stage1, ucount, st);
   ctx->launches++;
-  for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(s, ctx->join_ev[i], 0);
+  if (any_long)
+    for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(s, ctx->join_ev[i], 0);
   stage_end(ctx, CM_STAGE_TILES, s);
 
   // cxadj = exclusive scan of ucount; d_sizes[1] = m'.
@@ -1014,16 +1031,19 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
 
   // Every row's unique entries to their final place.
   stage_begin(ctx, s);
-  cudaEventRecord(ctx->fork_ev, s);
-  cudaStreamWaitEvent(ctx->aux[0], ctx->fork_ev, 0);
-  k_long_copy<<<grid_for(sms * 4, m / kLongThr), 256, 0, ctx->aux[0]>>>(long_list, chunk_row, eoff, ctr, mid_list, mid_ctr, (int)mid_cap,
-                                                 stage0, stage1, chunk_cnt, ucount, coarse->xadj, coarse->adjncy,
-                                                 coarse->adjwgt);
-  cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
-  k_copy_tiles<<<(unsigned)((ntiles + kCopyGroup - 1) / kCopyGroup), kCopyThreads, 0, s>>>(eoff, d_sizes, first_row, ucount, coarse->xadj, stage1,
-                                                         coarse->adjncy, coarse->adjwgt);
-  ctx->launches += 2;
-  cudaStreamWaitEvent(s, ctx->join_ev[0], 0);
+  if (any_long) {
+    cudaEventRecord(ctx->fork_ev, s);
+    cudaStreamWaitEvent(ctx->aux[0], ctx->fork_ev, 0);
+    k_long_copy<<<grid_for(sms * 4, m / kLongThr), 256, 0, ctx->aux[0]>>>(
+        long_list, chunk_row, eoff, ctr, mid_list, mid_ctr, (int)mid_cap, stage0, stage1, chunk_cnt, ucount,
+        coarse->xadj, coarse->adjncy, coarse->adjwgt);
+    cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
+    ctx->launches++;
+  }
+  k_copy_tiles<<<(unsigned)((ntiles + kCopyGroup - 1) / kCopyGroup), kCopyThreads, 0, s>>>(
+      eoff, d_sizes, first_row, ucount, coarse->xadj, stage1, coarse->adjncy, coarse->adjwgt);
+  ctx->launches++;
+  if (any_long) cudaStreamWaitEvent(s, ctx->join_ev[0], 0);
   stage_end(ctx, CM_STAGE_COPY, s);
   return check_launch(ctx, "contract");
 }

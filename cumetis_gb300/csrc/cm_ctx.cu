@@ -136,13 +136,23 @@ __global__ void k_selftest_wait(unsigned long long *status, DevStatus *st) {
   lookback_exclusive(status, 1, 1ull, st);
 }
 
-__global__ void k_sum_i32(const int *a, long long n, unsigned long long *out) {
-  unsigned long long s = 0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    s += (unsigned long long)(long long)a[i];
+// Input statistics of a device graph: out[0] = the vertex weights' sum,
+// out[1] = the largest degree (bounds the contraction's expanded rows).
+__global__ void k_input_stats(const int *vwgt, const int *xadj, long long n, unsigned long long *out) {
+  unsigned long long s = 0, d = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    s += (unsigned long long)(long long)vwgt[i];
+    d = max(d, (unsigned long long)(unsigned)(xadj[i + 1] - xadj[i]));
+  }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    d = max(d, __shfl_xor_sync(0xffffffffu, d, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(out, s);
+    atomicMax(out + 1, d);
+  }
 }
 
 }  // namespace
@@ -360,7 +370,7 @@ extern "C" int cm_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *d_m
   if (rc) return rc;
   ws_reset(ctx);
   if ((rc = ws_ensure(ctx, contract_ws_bytes(fine->nvtxs, fine->nedges)))) return rc;
-  return launch_contract(ctx, fine, d_match, d_cmap, coarse, d_sizes, (cudaStream_t)stream);
+  return launch_contract(ctx, fine, d_match, d_cmap, coarse, d_sizes, (cudaStream_t)stream, INT64_MAX);
 }
 
 // ---------------------------------------------------------------------------
@@ -447,6 +457,10 @@ extern "C" int cm_coarsen(cm_ctx *ctx, const cm_graph *g, int input_on_device, c
   // Level 0 on the device.
   cm_level L0;
   int64_t tvwgt = 0;
+  // Upper bound of the next contraction's expanded row length (twice the
+  // largest degree): the contraction skips the kernels of row classes that
+  // cannot occur.
+  int64_t row_bound = 0;
   if (input_on_device) {
     L0.g = *g;
     L0.owns_graph = false;
@@ -457,15 +471,16 @@ extern "C" int cm_coarsen(cm_ctx *ctx, const cm_graph *g, int input_on_device, c
     L0.block = p;
     L0.match = (int32_t *)p;
     L0.cmap = (int32_t *)(p + bv);
-    unsigned long long *d_sum = (unsigned long long *)ws_take(ctx, 8);
-    cudaMemsetAsync(d_sum, 0, 8, s);
-    k_sum_i32<<<std::max(1, ctx->num_sms * 4), 256, 0, s>>>(g->vwgt, n0, d_sum);
+    unsigned long long *d_stats = (unsigned long long *)ws_take(ctx, 16);
+    cudaMemsetAsync(d_stats, 0, 16, s);
+    k_input_stats<<<std::max(1, ctx->num_sms * 4), 256, 0, s>>>(g->vwgt, g->xadj, n0, d_stats);
     ctx->launches++;
-    unsigned long long hs = 0;
-    if ((rc = cuda_status(cudaMemcpyAsync(&hs, d_sum, 8, cudaMemcpyDeviceToHost, s), "tvwgt readback")) ||
-        (rc = stream_wait(ctx, s, "tvwgt sync")))
+    unsigned long long *hs = reinterpret_cast<unsigned long long *>(ctx->h_small);
+    if ((rc = cuda_status(cudaMemcpyAsync(hs, d_stats, 16, cudaMemcpyDeviceToHost, s), "input stats readback")) ||
+        (rc = stream_wait(ctx, s, "input stats sync")))
       return fail(rc);
-    tvwgt = (int64_t)hs;
+    tvwgt = (int64_t)hs[0];
+    row_bound = 2 * (int64_t)hs[1];
   } else {
     if ((rc = alloc_level(L0, n0, m0, ctx->pool, s))) return fail(rc);
     L0.g.nvtxs = (int32_t)n0;
@@ -475,7 +490,12 @@ extern "C" int cm_coarsen(cm_ctx *ctx, const cm_graph *g, int input_on_device, c
     cudaMemcpyAsync(L0.g.adjncy, g->adjncy, m0 * 4, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(L0.g.adjwgt, g->adjwgt, m0 * 4, cudaMemcpyHostToDevice, s);
     if ((rc = cuda_status(cudaGetLastError(), "input upload"))) return fail(rc);
-    for (int64_t i = 0; i < n0; ++i) tvwgt += g->vwgt[i];
+    int64_t maxdeg = 0;
+    for (int64_t i = 0; i < n0; ++i) {
+      tvwgt += g->vwgt[i];
+      maxdeg = std::max<int64_t>(maxdeg, (int64_t)g->xadj[i + 1] - g->xadj[i]);
+    }
+    row_bound = 2 * maxdeg;
   }
   h->levels.push_back(L0);
   // maxvwgt = (int)(1.5 * tvwgt / Coarsen_threshold), cuMetis.cu:1828
@@ -494,7 +514,7 @@ extern "C" int cm_coarsen(cm_ctx *ctx, const cm_graph *g, int input_on_device, c
       return fail(rc);
     }
     ctx->ws_used = level_ws_off;
-    if ((rc = launch_contract(ctx, &F.g, F.match, F.cmap, &C.g, sizes, s))) {
+    if ((rc = launch_contract(ctx, &F.g, F.match, F.cmap, &C.g, sizes, s, row_bound))) {
       cudaFreeAsync(C.block, s);
       return fail(rc);
     }
@@ -509,6 +529,9 @@ extern "C" int cm_coarsen(cm_ctx *ctx, const cm_graph *g, int input_on_device, c
       return fail(rc ? rc : CM_ERR_CUDA);
     }
     h->rounds.push_back(ctx->h_status->rounds);
+    // a coarse row holds at most its expanded length: the next level's
+    // degrees are at most this level's longest expanded row
+    row_bound = 2 * (int64_t)ctx->h_status->max_row;
     C.g.nvtxs = hsz[0];
     C.g.nedges = hsz[1];
     h->levels.push_back(C);

@@ -86,7 +86,9 @@ int launch_cmap(cm_ctx *ctx, int32_t n, const int32_t *xadj, const int32_t *vwgt
                 int32_t *long_list, int32_t long_threshold, int32_t long_chunk, unsigned long long *d_long_ctr,
                 int32_t *chunk_row, int32_t *first_row, int32_t tile_diag, int32_t *mid_list, int32_t *mid_ctr,
                 int32_t mid_cap, void *row_meta, cudaStream_t s);
+// row_bound: an upper bound of the longest expanded coarse row (INT64_MAX
+// when unknown); kernels of row classes above it are not launched.
 int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int32_t *cmap, cm_graph *coarse,
-                    int32_t *d_sizes, cudaStream_t s);
+                    int32_t *d_sizes, cudaStream_t s, int64_t row_bound);
 
 }  // namespace cm
