@@ -31,6 +31,7 @@ PARAMS = [
     ("CM_FIRST_MINBLOCKS", 8, [4, 6, 8], "cm_match.cu"),     # first-round kernel: blocks per SM (register cap)
     ("CM_FIRST_KEEP_SHORT", 2, [1, 2, 4], "cm_match.cu"),    # candidates the first round keeps (lane rows)
     ("CM_FIRST_KEEP_CHUNK", 2, [1, 2, 4], "cm_match.cu"),    # ... and per chunked row
+    ("CM_TAIL_ITEMS", 4096, [1024, 4096, 16384], "cm_match.cu"),  # rounds this small run in one block
     ("CM_LONG_THR", 1024, [512, 1024, 2048], "cm_contract.cu"),  # tile / long-row threshold
     ("CM_CHUNK", 8192, [4096, 8192], "cm_contract.cu"),      # long-row segment (chunk) size
     ("CM_TILE_DIAG", 512, [511, 512, 1023], "cm_contract.cu"),  # tile size (rows + entries)

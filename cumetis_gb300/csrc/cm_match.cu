@@ -59,6 +59,13 @@ constexpr int kChunk = CM_MATCH_CHUNK;
 static_assert(kSerialDeg == 8 || kSerialDeg == 16, "CM_SERIAL_DEG: 8 or 16");
 static_assert(kChunk == 128 || kChunk == 256 || kChunk == 512, "CM_MATCH_CHUNK: 128, 256 or 512");
 constexpr int kTop = 4;          // cached candidates per vertex
+// Tail mode (one block runs the remaining rounds) once a round has at most
+// kTailItems vertices to scan, commit or filter and kTailChunks row chunks.
+#ifndef CM_TAIL_ITEMS
+#define CM_TAIL_ITEMS 4096
+#endif
+constexpr long long kTailItems = CM_TAIL_ITEMS;
+constexpr int kTailChunks = 64;
 constexpr int kNotScanned = -2;  // top[v*kTop] before the first scan
 constexpr int kUnknown = -3;     // cache slot not computed (the first scan keeps only the best)
 // Candidates the first-round scans keep when every edge is eligible: short
@@ -545,6 +552,12 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
   };
   trace(0, 0, global_timer_ns());
 
+  // Tail mode: once a round's lists are small enough for one block, the
+  // other blocks return and block 0 runs the remaining rounds alone with
+  // block barriers instead of grid barriers (the rounds converge to the same
+  // matching whatever the schedule).  All blocks decide it alike: from the
+  // counters, read after a grid barrier.
+  bool tail = false;
   int round = 0;
   for (;; ++round) {
     const int par = round & 1;
@@ -556,6 +569,22 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
     const long long nact = round == 0 ? n : __ldcg(a.nact + par);
     const unsigned long long bc = __ldcg(a.big + par);
     const int nbig = (int)(bc >> 32), nchunks = (int)(bc & 0xffffffffu);
+    if (!tail && round > 0 && nsmall + nbig + nupd <= kTailItems && nchunks <= kTailChunks && nact <= kTailItems) {
+      tail = true;
+      if (blockIdx.x != 0) return;
+    }
+    // this round's thread, warp and block indices (block 0 alone in tail mode)
+    const long long gth = tail ? (long long)threadIdx.x : gthread;
+    const long long nth = tail ? (long long)blockDim.x : nthreads;
+    const int gw = tail ? (int)(threadIdx.x >> 5) : gwarp;
+    const int nw = tail ? (int)(blockDim.x >> 5) : nwarps;
+    const int bid = tail ? 0 : (int)blockIdx.x;
+    const int nblk = tail ? 1 : (int)gridDim.x;
+    auto barrier = [&]() -> bool {
+      if (!tail) return grid_barrier(st, gridDim.x);
+      __syncthreads();
+      return ld_relaxed(&st->error) == 0;
+    };
     if (round == 0) trace(0, 1, global_timer_ns());
     trace(round + 1, 0, global_timer_ns());
     trace(round + 1, 4, (unsigned long long)nsmall);
@@ -564,10 +593,10 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
     trace(round + 1, 7, (unsigned long long)nupd);
     if (nsmall == 0 && nbig == 0 && nupd == 0) break;
     if (round >= a.max_rounds) {
-      if (gthread == 0) record_error(st, CM_ERR_LIMIT, ERR_SITE_ROUNDS);
+      if (gth == 0) record_error(st, CM_ERR_LIMIT, ERR_SITE_ROUNDS);
       break;
     }
-    if (gthread == 0) {  // the next round's lists start empty
+    if (gth == 0) {  // the next round's lists start empty
       a.nsmall[par ^ 1] = 0;
       a.nupd[par ^ 1] = 0;
       a.nact[par ^ 1] = 0;
@@ -578,14 +607,14 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
     const bool first = round == 0;
 
     // ---- phase A: full scans (the first round's ran in k_match_first) ---------
-    if (!first) phase_a<H>(a, S, false, false, nsmall, nchunks, gwarp, nwarps, lane);
-    if (!grid_barrier(st, gridDim.x)) return;
+    if (!first) phase_a<H>(a, S, false, false, nsmall, nchunks, gw, nw, lane);
+    if (!barrier()) return;
     trace(round + 1, 1, global_timer_ns());
 
     // ---- phase B: commit mutual pairs ----------------------------------------
     // Candidates that changed this round: short scans, chunked scans, cache updates.
     const long long tot_b = nsmall + nbig + nupd;
-    for (long long i = gthread; i < tot_b; i += nthreads) {
+    for (long long i = gth; i < tot_b; i += nth) {
       int v;
       if (i < nsmall) {
         v = first ? (int)i : __ldcg(S.small + i);
@@ -605,13 +634,13 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
       a.m2[v] = p;
       a.m2[p] = v;
     }
-    if (!grid_barrier(st, gridDim.x)) return;
+    if (!barrier()) return;
     trace(round + 1, 2, global_timer_ns());
 
     // ---- phase C: filter the active list, refresh stale pointers -------------
     // Blocks take kMatchThreads * kCU consecutive entries (block-wide appends).
     const long long span = (long long)kMatchThreads * kCU;
-    for (long long b0 = (long long)blockIdx.x * span; b0 < nact; b0 += (long long)gridDim.x * span) {
+    for (long long b0 = (long long)bid * span; b0 < nact; b0 += (long long)nblk * span) {
       int x[kCU], p[kCU], sx[kCU], sp[kCU];
 #pragma unroll
       for (int u = 0; u < kCU; ++u) {
@@ -675,14 +704,19 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
 #pragma unroll
       for (int u = 0; u < kCU; ++u) append_scan(a, par ^ 1, scan[u] && !small[u], x[u], xs[u], deg[u]);
     }
-    if (!grid_barrier(st, gridDim.x)) return;
+    if (!barrier()) return;
     trace(round + 1, 3, global_timer_ns());
   }
-  for (long long v = gthread; v < n; v += nthreads)
-    if (__ldcg(a.m2 + v) < 0) a.m2[v] = (int)v;
+  // (unmatched vertices become singletons in k_match_finish)
   if (gthread == 0) st->rounds = round;
   trace(0, 3, global_timer_ns());
   trace(0, 4, (unsigned long long)round);
+}
+
+// After the rounds: every vertex still unmatched is a singleton.
+__global__ void k_match_finish(int n, int *__restrict__ m2) {
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x)
+    if (m2[v] < 0) m2[v] = (int)v;
 }
 
 int64_t max_chunks(int64_t n, int64_t m) { return m / kChunk + n + 64; }
@@ -762,9 +796,13 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
   }
   ctx->launches += 2;
   cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kMatchThreads), args, 0, s);
+  if (e != cudaSuccess) {
+    stage_end(ctx, CM_STAGE_MATCH, s);
+    return cuda_status(e, "cm_match launch");
+  }
+  k_match_finish<<<(unsigned)std::min<int64_t>((int64_t)ctx->num_sms * 4, n / 256 + 1), 256, 0, s>>>(n, d_match);
   stage_end(ctx, CM_STAGE_MATCH, s);
-  if (e != cudaSuccess) return cuda_status(e, "cm_match launch");
-  ctx->launches++;
+  ctx->launches += 2;
   return CM_OK;
 }
 
