@@ -12,8 +12,11 @@
 // edges, so mutual-proposal rounds converge to the unique greedy matching of
 // that order whatever the schedule.
 //
-// One persistent cooperative kernel (one 1024-thread block per SM) runs all
-// rounds; a round has three phases separated by grid barriers:
+// k_match_prep initialises the state, k_match_first runs the first round's
+// scans at high occupancy, and one persistent cooperative kernel (1024-thread
+// blocks, at most one per SM) runs the rounds; a round has three phases
+// separated by grid barriers (block barriers once a round fits one block, the
+// tail mode), and k_match_finish makes the unmatched vertices singletons:
 //   A  full scans: every vertex in the round's scan list computes its kTop
 //      best eligible unmatched candidates (cached) and points at the first.
 //      Rows of <= kSerialDeg entries: one lane each; longer rows: kChunk-entry
