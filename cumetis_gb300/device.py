@@ -5,7 +5,7 @@ import ctypes
 
 import numpy as np
 
-from . import (CM_OK, CMError, Graph, DeviceGraph, cm_coarsen_params, cm_graph, lib, _check, MATCH_HEM,
+from . import (CMError, Graph, DeviceGraph, cm_coarsen_params, cm_graph, lib, _check, MATCH_HEM,
                MATCH_HEM_HASH)
 
 

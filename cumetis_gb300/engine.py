@@ -4,7 +4,7 @@ import ctypes
 
 import numpy as np
 
-from . import (Graph, cm_batch_stats, cm_graph, cm_job_info, cm_part_params, lib, _check, _np_p,
+from . import (cm_batch_stats, cm_graph, cm_job_info, cm_part_params, lib, _check, _np_p,
                MATCH_HEM_HASH)
 
 

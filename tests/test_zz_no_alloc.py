@@ -11,7 +11,6 @@ last so that a failure here never hides the other GPU tests.
 """
 import ctypes
 
-import numpy as np
 import pytest
 
 import cumetis_gb300 as cm
