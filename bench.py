@@ -477,7 +477,7 @@ def main():
         per_launch_bytes = group_bytes["k_match"] / nlev
         per_launch_ms = group_ms["k_match"] / nlev
         ach = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
-        roof = {"kernel": "k_match (with k_match_prep, k_match_first)", "bound": "hbm", "achieved": ach, "peak": peak,
+        roof = {"kernel": "k_match (with k_match_prep, k_match_first, k_match_finish)", "bound": "hbm", "achieved": ach, "peak": peak,
                 "unit": "GB/s",
                 "frac": ach / peak, "peak_kind": peak_kind, "traffic": traffic,
                 "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms}
