@@ -150,7 +150,7 @@ def run_reference(args, ws, rank):
     gen, k, desc = WORKLOADS[args.workload]
     g = gen(cm)
     og = O.CSR(g.xadj, g.adjncy, g.adjwgt, g.vwgt)
-    thr = cm.coarsen_threshold(g.nvtxs, k)
+    thr = args.coarsen_to or cm.coarsen_threshold(g.nvtxs, k)
     mv = O.maxvwgt_rule(int(g.vwgt.sum()), thr)
 
     def step():
@@ -191,11 +191,11 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline(g, k, budget_s=20.0):
+def cpu_baseline(g, k, budget_s=20.0, coarsen_to=0):
     from oracle import oracle as O
     import cumetis_gb300 as cm
     og = O.CSR(g.xadj, g.adjncy, g.adjwgt, g.vwgt)
-    thr = cm.coarsen_threshold(g.nvtxs, k)
+    thr = coarsen_to or cm.coarsen_threshold(g.nvtxs, k)
     mv = O.maxvwgt_rule(int(g.vwgt.sum()), thr)
     O.srand(1)
     t0 = time.perf_counter()
@@ -382,6 +382,8 @@ def main():
     ap.add_argument("--drain", type=float, default=10.0, help="serve: seconds to wait for admitted jobs")
     ap.add_argument("--mode", type=int, default=1,
                     help="matching tie order: 1 = edge hash (default), 0 = lower vertex id")
+    ap.add_argument("--coarsen-to", type=int, default=0,
+                    help="coarsening threshold in place of the reference's rule max(n/(20 log2 k), 30k)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) measurement")
     ap.add_argument("--e2e-pipes", type=int, default=4, help="host threads (contexts) taking alternate e2e steps")
@@ -403,7 +405,7 @@ def main():
     dev = "cuda:%d" % local
     gen, k, desc = WORKLOADS[args.workload]
     g = gen(cm)
-    thr = cm.coarsen_threshold(g.nvtxs, k)
+    thr = args.coarsen_to or cm.coarsen_threshold(g.nvtxs, k)
     ctx = cm.Context(local)
     ctx.reserve(g.nvtxs, g.nedges)
     dg = g.to_device(dev)
@@ -554,7 +556,7 @@ def main():
                        "stage_ms_per_step": per_step_ms, "stage_roofline": stage_roofline},
             "roofline": roof, "clocks": clk, "gpu_launches": launches, "e2e": e2e}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(g, k)
+        line["cpu_baseline"] = cpu_baseline(g, k, coarsen_to=args.coarsen_to)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
