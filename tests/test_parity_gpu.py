@@ -276,6 +276,29 @@ def test_coarsen_hierarchy_bitexact(ctx, mode):
         h.close()
 
 
+@pytest.mark.parametrize("mode", [0, 1])
+def test_coarsen_hierarchy_with_chunked_rows(ctx, mode):
+    """The level loop passes each level's row bound to the contraction,
+    which then skips row classes and merge passes above it: graphs whose
+    first levels have rows beyond the 8192-entry chunk (a 20,000-leaf star,
+    a skewed R-MAT), from host and from device input, bit-exact against the
+    oracle's level loop at every level."""
+    for g in (star(20000), _o(cm.gen_rmat(16, 32, a=0.6, b=0.15, c=0.15, seed=5))):
+        hg = cm.Graph(np.asarray(g.xadj, np.int32), np.asarray(g.adjncy, np.int32), np.asarray(g.adjwgt, np.int32),
+                      np.asarray(g.vwgt, np.int32))
+        thr = max(30, g.n // 50)
+        want = O.coarsen(g, thr, mode)
+        for src in (hg, hg.to_device()):
+            h = ctx.coarsen(src, thr, mode)
+            assert len(h) == len(want), (len(h), len(want))
+            for l, (wg, wm, wc) in enumerate(want):
+                hgl, hc, hm = h.copy_level(l)
+                assert_same_graph(_o(hgl), wg, "level %d" % l)
+                if wm is not None:
+                    assert np.array_equal(hm, wm) and np.array_equal(hc, wc), l
+            h.close()
+
+
 def test_coarsen_device_input(ctx):
     g = cm.gen_grid3d(20, 20, 20)
     want = O.coarsen(_o(g), 300)
