@@ -21,6 +21,7 @@
 // separation 3, seeded through the Park-Miller minimal standard generator).
 // Memory is owned by std::vector; the reference's arena allocator is not
 // needed.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -137,7 +138,12 @@ void randarrayofp(Admin &a, int n, int *p, int nshuffles, bool init) {
 // Max-priority queue with float keys and a locator per node (cu:1968-2237).
 class Queue {
  public:
-  explicit Queue(int maxnodes) : heap_(maxnodes), loc_(maxnodes, -1) {}
+  // Heap slots at or beyond the current size are never read, so only the
+  // locators are initialised.
+  explicit Queue(int maxnodes)
+      : heap_(new KV[maxnodes > 0 ? maxnodes : 1]), loc_(new int[maxnodes > 0 ? maxnodes : 1]) {
+    std::fill(loc_.get(), loc_.get() + maxnodes, -1);
+  }
   void insert(int node, int key) {
     const float k = (float)key;
     long i = nn_++;
@@ -243,8 +249,8 @@ class Queue {
     heap_[i] = {newkey, node};
     loc_[node] = i;
   }
-  std::vector<KV> heap_;
-  std::vector<long> loc_;
+  std::unique_ptr<KV[]> heap_;
+  std::unique_ptr<int[]> loc_;  // heap slot of each node, -1 when absent
   long nn_ = 0;
 };
 
@@ -468,7 +474,8 @@ void two_way_refine(Admin &a, HGraph &g, const float *ntpwgts, int iteration_num
   const int n = g.n;
   int *where = g.where.data(), *id = g.id.data(), *ed = g.ed.data(), *bndptr = g.bndptr.data(),
       *bndlist = g.bndlist.data(), *pwgts = g.pwgts;
-  std::vector<int> moved(n, -1), swaps(n), perm(n);
+  std::vector<int> moved(n, -1);
+  std::unique_ptr<int[]> swaps(new int[n > 0 ? n : 1]), perm(new int[n > 0 ? n : 1]);  // written before read
   int tpwgts[2];
   tpwgts[0] = g.tvwgt * ntpwgts[0];
   tpwgts[1] = g.tvwgt - tpwgts[0];
@@ -484,7 +491,7 @@ void two_way_refine(Admin &a, HGraph &g, const float *ntpwgts, int iteration_num
     newcut = mincut = initcut = g.mincut;
     int mindiff = std::abs(tpwgts[0] - pwgts[0]);
     int nbnd = g.nbnd;
-    randarrayofp(a, nbnd, perm.data(), nbnd, true);
+    randarrayofp(a, nbnd, perm.get(), nbnd, true);
     for (int ii = 0; ii < nbnd; ++ii) {
       const int i = perm[ii];
       queues[where[bndlist[i]]].insert(bndlist[i], ed[bndlist[i]] - id[bndlist[i]]);
