@@ -945,19 +945,22 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   const int sms = ctx->num_sms;
   const bool small_ids = n <= kSmallIdMaxN;
   const size_t tile_smem = small_ids ? sizeof(TileSmem<unsigned>) : sizeof(TileSmem<unsigned long long>);
-  if (small_ids)
-    cudaFuncSetAttribute(k_contract_tiles<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem);
-  else
+  if (!ctx->contract_attrs_set) {  // once per context (the attributes last for the process)
+    cudaFuncSetAttribute(k_contract_tiles<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(TileSmem<unsigned>));
     cudaFuncSetAttribute(k_contract_tiles<unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)tile_smem);
-  cudaFuncSetAttribute(k_mid_rows<kMidThreads0, 2 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sizeof(MidSmem<2 * kLongThr>));
-  cudaFuncSetAttribute(k_mid_rows<kMidThreads1, 4 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sizeof(MidSmem<4 * kLongThr>));
-  cudaFuncSetAttribute(k_mid_rows<1024, kChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)sizeof(MidSmem<kChunk>));
-  cudaFuncSetAttribute(k_long_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MidSmem<kChunk>));
-  cudaFuncSetAttribute(k_long_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MergeSmem));
+                         (int)sizeof(TileSmem<unsigned long long>));
+    cudaFuncSetAttribute(k_mid_rows<kMidThreads0, 2 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(MidSmem<2 * kLongThr>));
+    cudaFuncSetAttribute(k_mid_rows<kMidThreads1, 4 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(MidSmem<4 * kLongThr>));
+    cudaFuncSetAttribute(k_mid_rows<1024, kChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(MidSmem<kChunk>));
+    cudaFuncSetAttribute(k_long_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MidSmem<kChunk>));
+    cudaFuncSetAttribute(k_long_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MergeSmem));
+    if (int rc2 = check_launch(ctx, "contract: kernel attributes")) return rc2;
+    ctx->contract_attrs_set = true;
+  }
 
   // Long rows on the auxiliary streams (three size classes; the chunked
   // rows' sort, merge passes and dedup after the largest class) while the

@@ -44,6 +44,10 @@ struct cm_ctx {
   // frees the core for other host work (the engine's workers)
   bool blocking_waits = false;
   cudaEvent_t wait_ev = nullptr;
+  // launch set-up done once: the contraction kernels' shared-memory limits,
+  // the matching kernel's resident blocks per SM (per tie order)
+  bool contract_attrs_set = false;
+  int match_blocks_per_sm[2] = {0, 0};
 };
 
 namespace cm {

@@ -778,10 +778,14 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
   a.st = ctx->d_status;
   a.trace = ctx->d_trace;
   a.trace_rows = ctx->trace_rows;
-  int per_sm = 0;
-  const void *fn = mode == CM_MATCH_HEM_HASH ? (const void *)k_match<true> : (const void *)k_match<false>;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kMatchThreads, 0);
-  if (per_sm < 1) return cm_fail(CM_ERR_CUDA, "cm_match: kernel cannot be resident");
+  const int hm = mode == CM_MATCH_HEM_HASH ? 1 : 0;
+  const void *fn = hm ? (const void *)k_match<true> : (const void *)k_match<false>;
+  int &per_sm = ctx->match_blocks_per_sm[hm];  // queried once per context and tie order
+  if (per_sm == 0) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kMatchThreads, 0);
+  if (per_sm < 1) {
+    per_sm = 0;
+    return cm_fail(CM_ERR_CUDA, "cm_match: kernel cannot be resident");
+  }
   // Small graphs take a few SMs, so that kernels of other contexts (other
   // streams) can run beside this one; the kernel is grid-size agnostic.
   const int64_t want = (n + g->nedges) / kWorkPerBlock + 1;
