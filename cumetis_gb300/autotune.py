@@ -3,9 +3,9 @@
     python -m cumetis_gb300.autotune [--workload rmat22] [--steps 40] [--out cumetis_gb300/tuned.json]
 
 Each tuning parameter is a macro of one CUDA source (the warp-per-vertex
-threshold and the warp work-item size of the matching, the tile / long-row
-threshold, the tile size and the chunk size of the contraction, the block
-shapes of their kernels).  The search is coordinate descent from the current tuning file (or
+threshold and the warp work-item size of the matching, the longest row the
+contraction sorts in one-warp batches and its chunk size, the block shapes of
+their kernels).  The search is coordinate descent from the current tuning file (or
 the compiled-in defaults): for each parameter in turn every other candidate
 value is built as a library variant (only the source it belongs to is
 recompiled), timed with bench.py in a fresh process on the same workload,
@@ -32,16 +32,9 @@ PARAMS = [
     ("CM_FIRST_KEEP_SHORT", 2, [1, 2, 4], "cm_match.cu"),    # candidates the first round keeps (lane rows)
     ("CM_FIRST_KEEP_CHUNK", 2, [1, 2, 4], "cm_match.cu"),    # ... and per chunked row
     ("CM_TAIL_ITEMS", 4096, [1024, 4096, 16384], "cm_match.cu"),  # rounds this small run in one block
-    ("CM_LONG_THR", 1024, [512, 1024, 2048], "cm_contract.cu"),  # tile / long-row threshold
-    ("CM_CHUNK", 8192, [4096, 8192], "cm_contract.cu"),      # long-row segment (chunk) size
-    ("CM_TILE_DIAG", 512, [511, 512, 1023], "cm_contract.cu"),  # tile size (rows + entries)
-    ("CM_TILE_THREADS", 256, [128, 256], "cm_contract.cu"),
-    ("CM_TILE_E", 4, [2, 4, 8], "cm_contract.cu"),           # keys per lane of the tile sort's warp runs
-    ("CM_MID_THREADS0", 256, [128, 256, 512], "cm_contract.cu"),
-    ("CM_MID_THREADS1", 512, [256, 512, 1024], "cm_contract.cu"),
+    ("CM_TINY_MAX", 32, [16, 32, 64], "cm_contract.cu"),    # rows sorted in one-warp batches; larger rows by size class
+    ("CM_CHUNK", 8192, [4096, 8192], "cm_contract.cu"),      # huge-row segment (chunk) size
     ("CM_MERGE_THREADS", 256, [256, 512], "cm_contract.cu"),
-    ("CM_COPY_THREADS", 128, [128, 256], "cm_contract.cu"),
-    ("CM_HASH_SLACK2", 4, [3, 4], "cm_contract.cu"),
 ]
 DEFAULTS = {name: d for name, d, _, _ in PARAMS}
 SOURCE = {name: src for name, _, _, src in PARAMS}
@@ -50,7 +43,7 @@ CHECK_TESTS = "test_long_rows or test_contract_bitexact or test_coarsen_hierarch
 
 def valid(cfg):
     """The sources' static constraints on combinations."""
-    return 4 * cfg["CM_LONG_THR"] <= cfg["CM_CHUNK"]
+    return cfg["CM_CHUNK"] // cfg["CM_TINY_MAX"] <= 256  # at most eight size classes
 
 
 def defines_by_source(cfg):

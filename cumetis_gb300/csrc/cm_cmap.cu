@@ -26,9 +26,8 @@ __global__ void __launch_bounds__(kCmapThreads)
 k_cmap(int n, const int *__restrict__ xadj, const int *__restrict__ vwgt, const int *__restrict__ match,
        int *__restrict__ cmap, int *__restrict__ leader, int *__restrict__ cvwgt, int *__restrict__ eoff,
        int *__restrict__ d_cnvtxs, int *__restrict__ long_list, int long_thr, unsigned long long *long_ctr,
-       int long_chunk, int *__restrict__ chunk_row, int *__restrict__ first_row, int tile_diag,
-       int *__restrict__ mid_list, int *__restrict__ mid_ctr, int mid_cap, int4 *__restrict__ row_meta,
-       unsigned long long *__restrict__ lb, DevStatus *st) {
+       int long_chunk, int *__restrict__ chunk_row, int *__restrict__ class_list, int *__restrict__ class_ctr,
+       long long m_fine, int4 *__restrict__ row_meta, unsigned long long *__restrict__ lb, DevStatus *st) {
   __shared__ int s_tile;
   __shared__ unsigned long long s_warp[kCmapThreads / 32];
   __shared__ unsigned long long s_excl;
@@ -92,13 +91,6 @@ k_cmap(int n, const int *__restrict__ xadj, const int *__restrict__ vwgt, const 
       if (row_meta) row_meta[c] = make_int4(xv, dv, xu, L);
       cvwgt[c] = (int)((unsigned)vwgt[v] + (u != v ? (unsigned)vwgt[u] : 0u));
       eoff[c] = e;
-      if (first_row) {
-        // Contraction tiles cover diagonals [kD, (k+1)D) of (row + entry)
-        // space; tile k starts at the first row whose diagonal c+eoff[c] >= kD.
-        const long long d0 = (long long)c + e, d1 = d0 + 1 + L;
-        for (long long k = d0 / tile_diag + 1; k <= d1 / tile_diag; ++k) first_row[k] = c + 1;
-        if (c == 0) first_row[0] = 0;
-      }
       if (L > long_thr) {
         if (L > long_chunk) {  // sorted in chunks and merged
           const int nch = (L + long_chunk - 1) / long_chunk;
@@ -109,9 +101,9 @@ k_cmap(int n, const int *__restrict__ xadj, const int *__restrict__ vwgt, const 
           long_list[2 * idx + 1] = cbase;  // first chunk index of this row
           for (int j = 0; j < nch; ++j) chunk_row[cbase + j] = idx;
         } else {  // sorted whole by one block of the row's size class
-          const int cls = L <= 2 * long_thr ? 0 : (L <= 4 * long_thr ? 1 : 2);
-          const int idx = atomicAdd(mid_ctr + cls, 1);
-          mid_list[(size_t)cls * mid_cap + idx] = c;
+          const int cls = min(kRowClasses - 1, 31 - __clz((L - 1) / long_thr));
+          const int idx = atomicAdd(class_ctr + cls, 1);
+          class_list[class_offset(m_fine, long_thr, cls) + idx] = c;
         }
       }
       row_max = L > row_max ? L : row_max;
@@ -147,8 +139,8 @@ size_t cmap_ws_bytes(int64_t n) { return (size_t)((n + kCmapTile - 1) / kCmapTil
 int launch_cmap(cm_ctx *ctx, int32_t n, const int32_t *xadj, const int32_t *vwgt, const int32_t *match,
                 int32_t *cmap, int32_t *leader, int32_t *cvwgt, int32_t *eoff, int32_t *d_cnvtxs,
                 int32_t *long_list, int32_t long_threshold, int32_t long_chunk, unsigned long long *d_long_ctr,
-                int32_t *chunk_row, int32_t *first_row, int32_t tile_diag, int32_t *mid_list, int32_t *mid_ctr,
-                int32_t mid_cap, void *row_meta, cudaStream_t s) {
+                int32_t *chunk_row, int32_t *class_list, int32_t *class_ctr, int64_t m, void *row_meta,
+                cudaStream_t s) {
   if (n == 0) {
     cudaMemsetAsync(d_cnvtxs, 0, sizeof(int32_t), s);
     cudaMemsetAsync(eoff, 0, sizeof(int32_t), s);
@@ -161,9 +153,8 @@ int launch_cmap(cm_ctx *ctx, int32_t n, const int32_t *xadj, const int32_t *vwgt
   stage_begin(ctx, s);
   k_cmap<<<ntiles, kCmapThreads, 0, s>>>(n, xadj, vwgt, match, cmap, leader, cvwgt, eoff, d_cnvtxs, long_list,
                                           long_list ? long_threshold : INT32_MAX, d_long_ctr,
-                                          long_chunk > 0 ? long_chunk : 1, chunk_row, first_row,
-                                          tile_diag > 0 ? tile_diag : 1, mid_list, mid_ctr, mid_cap,
-                                          (int4 *)row_meta, lb, ctx->d_status);
+                                          long_chunk > 0 ? long_chunk : 1, chunk_row, class_list, class_ctr,
+                                          (long long)m, (int4 *)row_meta, lb, ctx->d_status);
   ctx->launches++;
   int blocks = ctx->num_sms * 8;
   k_cmap_followers<<<blocks, 256, 0, s>>>(n, match, cmap, ctx->d_status);
@@ -244,8 +235,8 @@ extern "C" int cm_build_cmap_noalloc(int32_t nvtxs, const int32_t *d_xadj, const
   // ticket and this call's tile words.
   cudaMemsetAsync(D.scratch, 0, (size_t)(kNoAllocStatusWords + ntiles + 1) * 8, s);
   k_cmap<<<ntiles, kCmapThreads, 0, s>>>(nvtxs, d_xadj, d_vwgt, d_match, d_cmap, d_leader, d_cvwgt, d_eoff, d_cnvtxs,
-                                          nullptr, INT32_MAX, nullptr, 1, nullptr, nullptr, 1, nullptr, nullptr, 0,
-                                          nullptr, lb, st);
+                                          nullptr, INT32_MAX, nullptr, 1, nullptr, nullptr, nullptr, 0, nullptr, lb,
+                                          st);
   k_cmap_followers<<<D.num_sms * 8, 256, 0, s>>>(nvtxs, d_match, d_cmap, st);
   return cuda_status(cudaGetLastError(), "cm_build_cmap_noalloc launch");
 }

@@ -12,20 +12,24 @@
 // loop cmap[x] == c, is sorted ascending by coarse id, and equal ids are merged
 // with their weights summed (int32, wrapping).
 //
-// Work split by expanded coarse-row length L = deg(leader) + deg(follower):
-//   L <= kLongThr : contraction tiles.  Tile k owns the rows whose diagonal
-//                   c + eoff[c] lies in [kD, (k+1)D) (D = kTileDiag), so a tile
-//                   holds <= D rows and < D + kLongThr entries.  One pass per
-//                   tile: gather, merge duplicates in a shared-memory hash set,
-//                   sort the unique (row, coarse id) keys, and write each row's
-//                   unique entries to a stage at its expanded offset eoff[c].
-//   L >  kLongThr : long rows, beside the tiles on auxiliary streams.  Rows up
-//                   to kChunk entries: one block merges and sorts a row (three
-//                   size classes).  Longer rows: chunks of kChunk entries are
-//                   sorted in shared memory into a global stage, merged pairwise
-//                   (merge path, one launch per pass) and deduplicated.
-// A scan of the rows' unique counts gives cxadj; two copy kernels then move
-// every row from the stage to its final place.
+// Every sort is a shared-memory LSD radix sort with private per-thread digit
+// counters (cm_sort.cuh), sized to the row: no comparison network, no hash,
+// no atomics in the ranking.  Work split by expanded coarse-row length
+// L = deg(leader) + deg(follower):
+//   L <= kTinyMax     : tiny units, one warp each.  Unit k owns the rows
+//                       whose diagonal (rows before + tiny entries before)
+//                       lies in [kD, (k+1)D) (D = kTinyDiag), so it holds
+//                       < 2D entries of <= D/2 rows; their (row, coarse id)
+//                       keys are sorted together.
+//   kTinyMax < L <= kChunk : one block per row, sized to the row's class
+//                       (powers of two from 64 to kChunk entries; one warp up
+//                       to 512 entries), coarse-id keys only.
+//   L > kChunk        : huge rows.  Chunks of kChunk entries are sorted,
+//                       merged pairwise (merge path, one launch per pass) and
+//                       deduplicated.
+// Every row leaves its unique entries in a stage at its expanded offset
+// eoff[c] and their number in ucount[c]; a scan of ucount gives cxadj, and
+// one warp per row moves the entries to their final place.
 #include <algorithm>
 
 #include "cm_ctx.h"
@@ -34,322 +38,416 @@
 namespace cm {
 namespace {
 
-#ifndef CM_TILE_THREADS
-#define CM_TILE_THREADS 256
+__host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v >> 1); }
+
+// Tiny units: rows of at most kTinyMax entries, D = kTinyDiag diagonals per
+// unit, one warp per unit (capacity 2D entries, at most D/2 non-empty rows).
+#ifndef CM_TINY_MAX
+#define CM_TINY_MAX 32
 #endif
-constexpr int kTileThreads = CM_TILE_THREADS;     // threads per contraction tile
-#ifndef CM_TILE_E
-#define CM_TILE_E 4
-#endif
-constexpr int kTileE = CM_TILE_E;                 // keys per lane in the tile sort's register runs
-// D, diagonals per tile (a tuning parameter).  A tile holds at most D rows,
-// so its row index needs kTileRowBits bits.
-#ifndef CM_TILE_DIAG
-#define CM_TILE_DIAG 512
-#endif
-constexpr int kTileDiag = CM_TILE_DIAG;
-// Rows longer than kLongThr take the long path; rows longer than kChunk are
-// sorted in kChunk-entry chunks and merged.  Both are tuning parameters (the
-// autotuner's choice lands here through the build).
-#ifndef CM_LONG_THR
-#define CM_LONG_THR 1024
-#endif
+constexpr int kTinyMax = CM_TINY_MAX;
+constexpr int kTinyDiag = 2 * kTinyMax;
+constexpr int kTinyCap = 2 * kTinyDiag;
+constexpr int kTinyItems = kTinyCap / 32;
+constexpr int kTinyRowsPerLane = kTinyDiag / 32;
+constexpr int kTinyMaxNz = kTinyDiag / 2;
+constexpr int kTinyRowBits = ilog2(kTinyMaxNz - 1) + 1;
+static_assert(kTinyMax == 16 || kTinyMax == 32 || kTinyMax == 64, "CM_TINY_MAX: 16, 32 or 64");
+// Rows longer than kChunk are sorted in kChunk-entry chunks and merged.
 #ifndef CM_CHUNK
 #define CM_CHUNK 8192
 #endif
-constexpr int kLongThr = CM_LONG_THR;
-constexpr int kTileCap = kTileDiag + kLongThr;    // a tile holds fewer entries than this
-constexpr int kChunk = CM_CHUNK;                  // long-row chunk (entries sorted per block)
-constexpr int kChunkThreads = 1024;
-static_assert(kLongThr == 512 || kLongThr == 1024 || kLongThr == 2048, "CM_LONG_THR: 512, 1024 or 2048");
-static_assert(kChunk == 4096 || kChunk == 8192, "CM_CHUNK: 4096 or 8192 (one block's shared memory)");
-static_assert(4 * kLongThr <= kChunk, "the size classes 2x and 4x CM_LONG_THR must fit a chunk");
-// Threads per block of the three size classes of rows between kLongThr and
-// kChunk entries ((T, 2T], (2T, 4T], (4T, kChunk] for T = kLongThr; with the
-// defaults 1025-2048, 2049-4096, 4097-8192).
-#ifndef CM_MID_THREADS0
-#define CM_MID_THREADS0 256
-#endif
-#ifndef CM_MID_THREADS1
-#define CM_MID_THREADS1 512
-#endif
-constexpr int kMidThreads0 = CM_MID_THREADS0, kMidThreads1 = CM_MID_THREADS1;
+constexpr int kChunk = CM_CHUNK;
+constexpr int kChunkThreads = 512;
+constexpr int kChunkItems = kChunk / kChunkThreads;
+static_assert(kChunk == 4096 || kChunk == 8192, "CM_CHUNK: 4096 or 8192");
+// Row classes k = 0 .. : kTinyMax * 2^k < L <= kTinyMax * 2^(k+1), up to
+// kChunk; the block of class k has max(32, cap / 16) threads.
+constexpr int kClasses = ilog2(kChunk / kTinyMax);
+static_assert(kClasses <= kRowClasses, "row classes");
+constexpr int class_cap_entries(int k) { return kTinyMax << (k + 1); }
+constexpr int class_threads(int k) { return class_cap_entries(k) / 16 < 32 ? 32 : class_cap_entries(k) / 16; }
+constexpr int class_items(int k) { return class_cap_entries(k) / class_threads(k); }
+constexpr int kCopyBatch = 4;  // stage loads in flight per thread before their stores
 
-// Composite key (tile-local row, coarse id).  32-bit when the coarse ids fit
-// the bits the row index leaves (kTileIdBits), else 64-bit.  All-ones is the
-// empty hash slot and the sort pad; no key reaches it: with D < 2^rowbits the
-// row field never reaches all-ones, with D = 2^rowbits the id field must not
-// (n < 2^idbits).
-__host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v >> 1); }
-constexpr int kTileRowBits = ilog2(kTileDiag - 1) + 1;  // rows 0 .. D-1
-constexpr int kTileIdBits = 32 - kTileRowBits;
-constexpr long long kSmallIdMaxN =                       // largest n with 32-bit keys
-    kTileDiag < (1 << kTileRowBits) ? (1ll << kTileIdBits) : (1ll << kTileIdBits) - 1;
-static_assert(kTileDiag >= 256 && kTileDiag <= 1024, "CM_TILE_DIAG: 256 .. 1024");
-template <typename K> struct KeyT;
-template <> struct KeyT<unsigned> {
-  static constexpr int kShift = kTileIdBits;
-  static constexpr unsigned kIdMask = (1u << kTileIdBits) - 1;
-  static __device__ __forceinline__ unsigned make(int r, unsigned id) { return ((unsigned)r << kShift) | id; }
-  static __device__ __forceinline__ int row(unsigned k) { return (int)(k >> kShift); }
-  static __device__ __forceinline__ unsigned id(unsigned k) { return k & kIdMask; }
-};
-template <> struct KeyT<unsigned long long> {
-  static __device__ __forceinline__ unsigned long long make(int r, unsigned id) {
-    return ((unsigned long long)r << 32) | id;
-  }
-  static __device__ __forceinline__ int row(unsigned long long k) { return (int)(k >> 32); }
-  static __device__ __forceinline__ unsigned id(unsigned long long k) { return (unsigned)k; }
-};
-
-__device__ __forceinline__ int upper_bound_smem(const int *a, int n, int x) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (a[mid] <= x) lo = mid + 1;
-    else hi = mid;
-  }
-  return lo;
-}
-
-// Gathers entry o (0 <= o < L) of the expanded row: the leader's entries first
+// Expanded entry o (0 <= o < L) of a coarse row: the leader's entries first
 // (as find_cnvtxsedge_original places them, cuMetis.cu:1014-1020).
 __device__ __forceinline__ int expanded_src(int o, int xl, int dl, int xf) { return o < dl ? xl + o : xf + (o - dl); }
 
-// ---------------------------------------------------------------------------
-// Shared-memory hash set with weight sums (one per tile or per row).  Keys are
-// inserted with atomicCAS into open-addressed slots (linear probing, Fibonacci
-// hashing); the weight of every copy of a key is added to its slot.  A slot,
-// once set, never changes, so a plain read that finds the key is final.
-// ---------------------------------------------------------------------------
+// Bits of a coarse id (ids < nc).
+__device__ __forceinline__ int id_bits(int nc) { return nc > 1 ? 32 - __clz(nc - 1) : 0; }
+
+// Appends (key, w) for the lanes with keep set to a padded sort buffer at a
+// shared counter (warp-aggregated; the order within the buffer is arbitrary).
 template <typename K>
-__device__ __forceinline__ unsigned hash_home(K key, int shift) {
-  return (unsigned)(((unsigned long long)key * 0x9E3779B97F4A7C15ull) >> shift);
-}
-
-template <typename K>
-__device__ __forceinline__ void hash_add(K *hk, int *hw, unsigned hmask, int shift, K key, int w) {
-  const K empty = ~(K)0;
-  unsigned h = hash_home(key, shift);
-  for (unsigned p = 0; p <= hmask; ++p) {
-    K old = hk[h];
-    if (old == empty) old = atomicCAS(&hk[h], empty, key);
-    if (old == empty || old == key) {
-      atomicAdd(&hw[h], w);
-      return;
-    }
-    h = (h + 1) & hmask;
-  }
-}
-
-// Weight sum of a key known to be in the set.
-template <typename K>
-__device__ __forceinline__ int hash_get(const K *hk, const int *hw, unsigned hmask, int shift, K key) {
-  unsigned h = hash_home(key, shift);
-  for (unsigned p = 0; p <= hmask; ++p) {
-    if (hk[h] == key) return hw[h];
-    h = (h + 1) & hmask;
-  }
-  return 0;
-}
-
-// Table size for n keys: the power of two >= kHashSlack2 * n / 2 (load at
-// most 2 / kHashSlack2; at least 64 slots, at most the cap); returns log2.
-#ifndef CM_HASH_SLACK2
-#define CM_HASH_SLACK2 4
-#endif
-constexpr int kHashSlack2 = CM_HASH_SLACK2;
-__device__ __forceinline__ int hash_log2(int n, int cap_log2) {
-  int lg = 6;
-  while (lg < cap_log2 && 2 * (1 << lg) < kHashSlack2 * n) ++lg;
-  return lg;
-}
-
-// Appends the set's keys to dst (arbitrary order, warp-aggregated); returns
-// their number.  All NT threads call it; *ctr is a shared counter set to 0.
-template <typename K, int NT>
-__device__ __forceinline__ int hash_compact(const K *hk, int hsize, K *dst, int *ctr) {
-  const K empty = ~(K)0;
+__device__ __forceinline__ void append_pair(SortPair<K> *buf, int *ctr, bool keep, K key, int w) {
   const int lane = threadIdx.x & 31;
-  for (int i0 = threadIdx.x - lane; i0 < hsize; i0 += NT) {
-    const int i = i0 + lane;
-    const K k = i < hsize ? hk[i] : empty;
-    const unsigned m = __ballot_sync(0xffffffffu, k != empty);
-    int base = 0;
-    if (lane == 0 && m) base = atomicAdd(ctr, __popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (k != empty) dst[padk<K>(base + __popc(m & ((1u << lane) - 1)))] = k;
-  }
-  __syncthreads();
-  const int n = *ctr;
-  __syncthreads();
-  return n;
+  const unsigned m = __ballot_sync(0xffffffffu, keep);
+  int base = 0;
+  if (lane == 0 && m) base = atomicAdd(ctr, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (keep) buf[rslot(base + __popc(m & lanemask_lt()))] = make_pair_kv<K>(key, w);
 }
 
 // ---------------------------------------------------------------------------
-// Contraction tiles
+// One block sorts a segment of one row (class rows and chunks)
 // ---------------------------------------------------------------------------
-// Table slots: the power of two of at least 4/3 kTileCap (load <= 3/4; 2048
-// for the default kTileCap of 1536).
-constexpr int kTileHashLog2 = ilog2((4 * kTileCap + 2) / 3 - 1) + 1;
-constexpr int kTileHash = 1 << kTileHashLog2;
-static_assert(kTileHash > kTileCap, "tile hash must have a free slot for every entry");
-
-struct TileRows {
-  int r_xl[kTileDiag], r_dl[kTileDiag], r_xf[kTileDiag], r_start[kTileDiag];
-};
-
-template <typename K>
-struct TileSmem {
-  union {
-    TileRows T;                                   // gather
-    K keys[2][padded_k<K>(((kTileCap + 32 * kTileE - 1) / (32 * kTileE)) * 32 * kTileE)];  // sort of the unique keys
-  } u;
-  K hk[kTileHash];
-  int hw[kTileHash];
-  int r_out[kTileDiag];                           // staging offset eoff[c] of a short row, -1 for a long row
-  int ustart[kTileDiag + 1];                      // first sorted unique key of each row
-  int scan[kTileThreads / 32 + 1];
+template <int NT, int ITEMS>
+struct SegSmem {
+  SortPair<unsigned> work[rslots(NT * ITEMS)];
+  SortScratch<NT> sc;
   int ctr;
 };
 
-// Rows [clo, clo+R) of tile t (rows whose diagonal c + eoff[c] lies in
-// [tD, (t+1)D)); loads their metadata and lays the short rows' entries out
-// back to back (long rows take no space).  Returns the number of entries.
-template <typename K>
-__device__ __forceinline__ int tile_rows(TileSmem<K> &S, int tile, int nc, long long dend,
-                                         const int *__restrict__ first_row, const int4 *__restrict__ row_meta,
-                                         const int *__restrict__ eoff, int &clo, int &R, DevStatus *st) {
-  const int tid = threadIdx.x;
-  const long long last = dend / kTileDiag;
-  clo = tile <= last ? first_row[tile] : nc;
-  const int chi = tile + 1 <= last ? first_row[tile + 1] : nc;
-  R = chi - clo;
-  if (R < 0 || R > kTileDiag) {  // inconsistent tile map: report, touch nothing
-    if (tid == 0) record_error(st, CM_ERR_INVALID, ERR_SITE_BOUNDS);
-    R = 0;
-  }
-  if (R == 0) return 0;  // a tile inside a long row's diagonal span holds no row
-  constexpr int kRowsPerThread = (kTileDiag + kTileThreads - 1) / kTileThreads;
-  int lens[kRowsPerThread];
-  int mysum = 0;
+// Writes the unique entries (coarse id, summed weight) of entries
+// [cs, cs + cnt) of coarse row c's expanded row (metadata md), ascending by
+// id, self loops dropped, to dst[0..U).  Returns U.  cnt <= NT * ITEMS; all
+// NT threads call it; it ends with a block barrier.
+template <int NT, int ITEMS>
+__device__ __forceinline__ int segment_sorted_unique(SegSmem<NT, ITEMS> &S, int c, const int4 &md, int cs, int cnt,
+                                                     int idbits, const int *__restrict__ adjncy,
+                                                     const int *__restrict__ adjwgt, const int *__restrict__ cmap,
+                                                     int2 *__restrict__ dst) {
+  constexpr int kBatch = ITEMS < 4 ? ITEMS : 4;
+  if (threadIdx.x == 0) S.ctr = 0;
+  __syncthreads();
+  for (int b = 0; b < cnt; b += kBatch * NT) {
+    int src[kBatch], x[kBatch], w[kBatch];
 #pragma unroll
-  for (int i = 0; i < kRowsPerThread; ++i) {
-    const int r = tid * kRowsPerThread + i;
-    int len = 0;
-    if (r < R) {
-      const int4 md = row_meta[clo + r];  // (leader start, leader length, follower start, length)
-      S.u.T.r_xl[r] = md.x;
-      S.u.T.r_dl[r] = md.y;
-      S.u.T.r_xf[r] = md.z;
-      const bool lng = md.w > kLongThr;
-      S.r_out[r] = lng ? -1 : eoff[clo + r];
-      len = lng ? 0 : md.w;
+    for (int u = 0; u < kBatch; ++u) {
+      const int t = b + u * NT + (int)threadIdx.x;
+      src[u] = t < cnt ? expanded_src(cs + t, md.x, md.y, md.z) : -1;
     }
-    lens[i] = len;
-    mysum += len;
-  }
-  int ntot;
-  int ex = block_exclusive_scan<kTileThreads>(mysum, S.scan, &ntot);
-  const bool overflow = ntot > kTileCap;
-  if (overflow) {
-    if (tid == 0) record_error(st, CM_ERR_INVALID, ERR_SITE_BOUNDS);
-    ntot = 0;
-  }
 #pragma unroll
-  for (int i = 0; i < kRowsPerThread; ++i) {
-    const int r = tid * kRowsPerThread + i;
-    if (r < R) {
-      S.u.T.r_start[r] = overflow ? 0 : ex;
-      if (overflow) S.r_out[r] = -1;
+    for (int u = 0; u < kBatch; ++u) {
+      x[u] = src[u] >= 0 ? __ldcs(adjncy + src[u]) : 0;
+      w[u] = src[u] >= 0 ? __ldcs(adjwgt + src[u]) : 0;
     }
-    ex += lens[i];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : c;
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) append_pair<unsigned>(S.work, &S.ctr, x[u] != c, (unsigned)x[u], w[u]);
   }
   __syncthreads();
-  return ntot;
+  const int n = S.ctr;
+  block_radix_sort<unsigned, NT, ITEMS>(S.work, S.sc, n, idbits);
+  return block_unique_emit<unsigned, NT, ITEMS>(S.work, n, S.sc, [&](unsigned key, int sum, int q) {
+    dst[q] = make_int2((int)key, sum);
+  });
 }
 
-// One pass per tile: gathers the short rows' expanded entries (row, coarse
-// id, weight), merges duplicates in a shared-memory hash set (self loops are
-// dropped), sorts the unique (row, id) keys, and writes each row's unique
-// entries, ascending by id with summed weights, to stage[eoff[c] ...) and
-// their number to ucount[c].
-template <typename K>
-__global__ void __launch_bounds__(kTileThreads)
-k_contract_tiles(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
-                 const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
-                 const int4 *__restrict__ row_meta, int2 *__restrict__ stage, int *__restrict__ ucount,
-                 DevStatus *st) {
-  using KT = KeyT<K>;
+// Rows of one size class: one block per row writes the row's unique entries
+// to stage[eoff[c] ...) and their number to ucount[c].
+template <int NT, int ITEMS>
+__global__ void __launch_bounds__(NT)
+k_class_rows(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
+             const int *__restrict__ eoff, const int4 *__restrict__ row_meta, const int *__restrict__ list,
+             const int *__restrict__ count, const int *d_cn, int2 *__restrict__ stage, int *__restrict__ ucount) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  TileSmem<K> &S = *reinterpret_cast<TileSmem<K> *>(smem_raw);
-  const int tid = threadIdx.x;
-  const int nc = *d_cn;
-  const long long dend = (long long)nc + eoff[nc];
-  int clo, R;
-  if (tid == 0) S.ctr = 0;
-  const int ntot = tile_rows(S, blockIdx.x, nc, dend, first_row, row_meta, eoff, clo, R, st);
-  if (ntot == 0) {  // no short-row entries (uniform): short rows here are empty
-    for (int r = tid; r < R; r += kTileThreads)
-      if (S.r_out[r] >= 0) ucount[clo + r] = 0;
-    return;
+  SegSmem<NT, ITEMS> &S = *reinterpret_cast<SegSmem<NT, ITEMS> *>(smem_raw);
+  const int nrows = *count;
+  const int idbits = id_bits(*d_cn);
+  for (int i = blockIdx.x; i < nrows; i += gridDim.x) {
+    const int c = list[i];
+    const int4 md = row_meta[c];
+    const int U = segment_sorted_unique<NT, ITEMS>(S, c, md, 0, min(md.w, NT * ITEMS), idbits, adjncy, adjwgt, cmap,
+                                                   stage + eoff[c]);
+    if (threadIdx.x == 0) ucount[c] = U;
   }
-  const int lg = hash_log2(ntot, kTileHashLog2);
-  const int hsize = 1 << lg, shift = 64 - lg;
-  const unsigned hmask = hsize - 1;
-  for (int i = tid; i < hsize; i += kTileThreads) {
-    S.hk[i] = ~(K)0;
-    S.hw[i] = 0;
+}
+
+// Passes a row of length L needs before its chunks form one sorted run.
+__host__ __device__ __forceinline__ int merge_passes(int L) {
+  int p = 0;
+  long long w = kChunk;
+  while (w < L) { w <<= 1; ++p; }
+  return p;
+}
+
+// Chunked rows carry packed entries (coarse id << 32 | weight) through the
+// merge passes.  Pad entries have the id kPadId, above every coarse id
+// (< 2^31 - 1), so they sort to the end of every merged run.
+constexpr unsigned kPadId = 0x7fffffffu;
+__device__ __forceinline__ unsigned long long pack_entry(int2 e) {
+  return ((unsigned long long)(unsigned)e.x << 32) | (unsigned)e.y;
+}
+__device__ __forceinline__ int2 unpack_entry(unsigned long long v) {
+  return make_int2((int)(unsigned)(v >> 32), (int)(unsigned)v);
+}
+
+// Rows longer than kChunk: each chunk of kChunk entries becomes one sorted run
+// in stage0 for the merge passes -- its unique entries (duplicates within the
+// chunk already merged, self loops dropped), then pad entries up to the
+// chunk's length, which sort after every coarse id and are skipped by the
+// dedup.  chunk_np[q] = the merge passes the chunk's row needs.
+__global__ void __launch_bounds__(kChunkThreads, 1)
+k_long_sort(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
+            const int *__restrict__ eoff, const int4 *__restrict__ row_meta, const int *__restrict__ long_list,
+            const int *__restrict__ chunk_row, const unsigned long long *long_ctr, const int *d_cn,
+            int2 *__restrict__ stage, int *__restrict__ ucount, int *__restrict__ chunk_np) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SegSmem<kChunkThreads, kChunkItems> &S = *reinterpret_cast<SegSmem<kChunkThreads, kChunkItems> *>(smem_raw);
+  const int nchunks = (int)(*long_ctr & 0xffffffffu);
+  const int idbits = id_bits(*d_cn);
+  for (int q = blockIdx.x; q < nchunks; q += gridDim.x) {
+    const int idx = chunk_row[q];
+    const int c = long_list[2 * idx];
+    const int4 md = row_meta[c];
+    const int j = q - long_list[2 * idx + 1];
+    const int cs = j * kChunk;
+    const int cnt = min(kChunk, md.w - cs);
+    if (j == 0 && threadIdx.x == 0) ucount[c] = 0;  // the dedup adds the chunks' counts
+    if (threadIdx.x == 0) chunk_np[q] = merge_passes(md.w);
+    int2 *dst = stage + eoff[c] + cs;
+    const int U = segment_sorted_unique<kChunkThreads, kChunkItems>(S, c, md, cs, cnt, idbits, adjncy, adjwgt, cmap,
+                                                                    dst);
+    for (int t = U + threadIdx.x; t < cnt; t += kChunkThreads) dst[t] = make_int2((int)kPadId, 0);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Unit map: first row of every tiny unit
+// ---------------------------------------------------------------------------
+constexpr int kMapThreads = 256, kMapItems = 8, kMapTile = kMapThreads * kMapItems;
+
+// Row c costs 1 + (L <= kTinyMax ? L : 0) diagonals; unit k starts at the
+// first row whose diagonal (the cost of the rows before it) is >= kD.  A
+// single-pass scan over the coarse rows (2048 per tile, decoupled
+// look-back).  *unit_last = the unit of the last row.
+__global__ void __launch_bounds__(kMapThreads)
+k_unit_map(const int *d_cn, const int *__restrict__ eoff, int *__restrict__ first_row, int *unit_last,
+           unsigned long long *lb, DevStatus *st) {
+  __shared__ int s_tile;
+  __shared__ unsigned long long s_warp[kMapThreads / 32];
+  __shared__ unsigned long long s_excl;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nc = *d_cn;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(lb, 1ull);
+  __syncthreads();
+  const int tile = s_tile;
+  if ((long long)tile * kMapTile >= nc) return;  // past the last row: nobody looks back at it
+  const long long base = (long long)tile * kMapTile + (long long)threadIdx.x * kMapItems;
+  int cost[kMapItems];
+  unsigned long long sum = 0;
+#pragma unroll
+  for (int i = 0; i < kMapItems; ++i) {
+    const long long c = base + i;
+    cost[i] = 0;
+    if (c < nc) {
+      const int L = eoff[c + 1] - eoff[c];
+      cost[i] = 1 + (L <= kTinyMax ? L : 0);
+    }
+    sum += (unsigned)cost[i];
+  }
+  const unsigned long long inc = warp_inclusive_scan_u64(sum);
+  if (lane == 31) s_warp[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    const unsigned long long x = lane < kMapThreads / 32 ? s_warp[lane] : 0ull;
+    const unsigned long long xi = warp_inclusive_scan_u64(x);
+    const unsigned long long agg = __shfl_sync(0xffffffffu, xi, kMapThreads / 32 - 1);
+    if (lane < kMapThreads / 32) s_warp[lane] = xi - x;
+    const unsigned long long ex = lookback_exclusive(lb, tile, agg, st);
+    if (lane == 0) s_excl = ex;
   }
   __syncthreads();
-  for (int e0 = tid; e0 < ntot; e0 += 4 * kTileThreads) {
-    int src[4], rr[4], id[4], w[4];
+  long long d0 = (long long)(s_excl + s_warp[wid] + inc - sum);
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int e = e0 + u * kTileThreads;
-      rr[u] = 0;
-      src[u] = -1;
-      if (e < ntot) {
-        const int r = upper_bound_smem(S.u.T.r_start, R, e) - 1;
-        rr[u] = r;
-        src[u] = expanded_src(e - S.u.T.r_start[r], S.u.T.r_xl[r], S.u.T.r_dl[r], S.u.T.r_xf[r]);
+  for (int i = 0; i < kMapItems; ++i) {
+    const long long c = base + i;
+    if (c >= nc) break;
+    const long long d1 = d0 + cost[i];
+    for (long long k = d0 / kTinyDiag + 1; k <= d1 / kTinyDiag; ++k) first_row[k] = (int)c + 1;
+    if (c == 0) first_row[0] = 0;
+    if (c == nc - 1) *unit_last = (int)(d0 / kTinyDiag);
+    d0 = d1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tiny units: one warp each
+// ---------------------------------------------------------------------------
+template <typename K>
+struct TinySmem {
+  SortPair<K> work[rslots(kTinyCap)];
+  SortScratch<32> sc;
+  int rstart[kTinyMaxNz], xl[kTinyMaxNz], dl[kTinyMaxNz], xf[kTinyMaxNz];
+  int rcount[kTinyMaxNz], rfirst[kTinyMaxNz], rdst[kTinyMaxNz];
+  unsigned char rowid[kTinyCap];  // sorted row of every gathered entry
+  unsigned char nz_row[kTinyMaxNz];
+  int ctr;
+};
+static_assert(kTinyMaxNz <= 256 && kTinyDiag <= 256, "tiny unit row ids are 8-bit");
+
+// One warp per unit (grid-stride over the units).  Per unit: the rows'
+// metadata, every entry's row (a max-scan of the rows' first entries), the
+// gather of (row << idbits | coarse id, weight) pairs without self loops, a
+// radix sort of the keys, and every run of equal keys written once, weights
+// summed, to stage[eoff[c] ...) of its row; ucount[c] = the row's unique
+// entries (0 for empty rows; rows above kTinyMax are counted by their class).
+template <typename K>
+__global__ void __launch_bounds__(32)
+k_tiny_units(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
+             const int *d_sizes, const int *__restrict__ first_row, const int *unit_last,
+             const int4 *__restrict__ row_meta, const int *__restrict__ eoff, int2 *__restrict__ stage,
+             int *__restrict__ ucount, DevStatus *st) {
+  constexpr int RPL = kTinyRowsPerLane;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TinySmem<K> &S = *reinterpret_cast<TinySmem<K> *>(smem_raw);
+  const int lane = threadIdx.x;
+  const unsigned below = lanemask_lt();
+  const int nc = d_sizes[0];
+  const int last = *unit_last;
+  const int idbits = id_bits(nc);
+  const unsigned idmask = idbits >= 32 ? 0xffffffffu : ((1u << idbits) - 1u);
+  for (int u = blockIdx.x; u <= last; u += gridDim.x) {
+    const int clo = first_row[u];
+    const int chi = u < last ? first_row[u + 1] : nc;
+    int R = chi - clo;
+    if (R < 0 || R > kTinyDiag) {  // inconsistent unit map: report, touch nothing
+      if (lane == 0) record_error(st, CM_ERR_INVALID, ERR_SITE_BOUNDS);
+      R = 0;
+    }
+    // ---- rows: metadata, sorted-row index, entry layout (lane l: rows RPL*l ..)
+    int len[RPL], jr[RPL], packed = 0;
+    int4 md[RPL];
+#pragma unroll
+    for (int i = 0; i < RPL; ++i) {
+      const int r = lane * RPL + i;
+      md[i] = make_int4(0, 0, 0, 0);
+      if (r < R) md[i] = row_meta[clo + r];
+      const bool tiny = r < R && md[i].w <= kTinyMax;
+      len[i] = tiny ? md[i].w : 0;
+      if (tiny && len[i] == 0) ucount[clo + r] = 0;
+      packed += (len[i] > 0 ? (1 << 16) : 0) + len[i];
+    }
+    const int incl = warp_inclusive_scan_i32(packed);
+    const int tot = __shfl_sync(0xffffffffu, incl, 31);
+    int ex = incl - packed;
+    int ntot = tot & 0xffff, nnz = tot >> 16;
+    if (ntot >= kTinyCap || nnz > kTinyMaxNz) {  // inconsistent row metadata: report, touch nothing
+      if (lane == 0) record_error(st, CM_ERR_INVALID, ERR_SITE_BOUNDS);
+      ntot = 0;
+      nnz = 0;
+#pragma unroll
+      for (int i = 0; i < RPL; ++i) len[i] = 0;
+    }
+#pragma unroll
+    for (int i = 0; i < RPL; ++i) {
+      jr[i] = -1;
+      if (len[i] > 0) {
+        const int j = ex >> 16, e0 = ex & 0xffff;
+        jr[i] = j;
+        S.rstart[j] = e0;
+        S.xl[j] = md[i].x;
+        S.dl[j] = md[i].y;
+        S.xf[j] = md[i].z;
+        S.nz_row[j] = (unsigned char)(lane * RPL + i);
+        S.rcount[j] = 0;
+        ex += (1 << 16) + len[i];
       }
     }
+    for (int e = lane; e < kTinyCap; e += 32) S.rowid[e] = 0;
+    if (lane == 0) S.ctr = 0;
+    __syncwarp();
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      id[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
-      w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
+    for (int i = 0; i < RPL; ++i)
+      if (jr[i] > 0) S.rowid[S.rstart[jr[i]]] = (unsigned char)jr[i];
+    __syncwarp();
+    {  // every entry's row: inclusive max-scan of the first-entry marks
+      unsigned v[kTinyItems], run = 0;
+#pragma unroll
+      for (int i = 0; i < kTinyItems; ++i) {
+        v[i] = S.rowid[lane * kTinyItems + i];
+        run = max(run, v[i]);
+      }
+      unsigned wmax = run;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, wmax, o);
+        if (lane >= o) wmax = max(wmax, y);
+      }
+      unsigned cur = __shfl_up_sync(0xffffffffu, wmax, 1);
+      if (lane == 0) cur = 0;
+      __syncwarp();
+#pragma unroll
+      for (int i = 0; i < kTinyItems; ++i) {
+        cur = max(cur, v[i]);
+        S.rowid[lane * kTinyItems + i] = (unsigned char)cur;
+      }
     }
+    __syncwarp();
+    // ---- gather (row << idbits | coarse id, weight), self loops dropped
+    {
+      int src[kTinyItems], x[kTinyItems], w[kTinyItems], jj[kTinyItems];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) id[u] = src[u] >= 0 ? cmap[id[u]] : 0;
+      for (int q = 0; q < kTinyItems; ++q) {
+        const int e = q * 32 + lane;
+        src[q] = -1;
+        jj[q] = 0;
+        if (e < ntot) {
+          const int j = S.rowid[e];
+          jj[q] = j;
+          src[q] = expanded_src(e - S.rstart[j], S.xl[j], S.dl[j], S.xf[j]);
+        }
+      }
 #pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (src[u] >= 0 && id[u] != clo + rr[u])
-        hash_add<K>(S.hk, S.hw, hmask, shift, KT::make(rr[u], (unsigned)id[u]), w[u]);
-  }
-  __syncthreads();  // gather done: the row table is dead, its space holds the keys
-  const int U = hash_compact<K, kTileThreads>(S.hk, hsize, S.u.keys[0], &S.ctr);
-  const int b = block_sort_keys<K, kTileThreads, kTileE>(S.u.keys[0], S.u.keys[1], U);
-  const K *sk = S.u.keys[b];
-  // first sorted key of each row: lower bound of (r, 0)
-  for (int r = tid; r <= R; r += kTileThreads) {
-    const K key = r < R ? KT::make(r, 0u) : ~(K)0;
-    int lo = 0, hi = U;
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (sk[padk<K>(mid)] < key) lo = mid + 1;
-      else hi = mid;
+      for (int q = 0; q < kTinyItems; ++q) {
+        x[q] = src[q] >= 0 ? __ldcs(adjncy + src[q]) : 0;
+        w[q] = src[q] >= 0 ? __ldcs(adjwgt + src[q]) : 0;
+      }
+#pragma unroll
+      for (int q = 0; q < kTinyItems; ++q) x[q] = src[q] >= 0 ? cmap[x[q]] : -1;
+#pragma unroll
+      for (int q = 0; q < kTinyItems; ++q) {
+        const bool keep = src[q] >= 0 && x[q] != clo + (int)S.nz_row[jj[q]];
+        append_pair<K>(S.work, &S.ctr, keep, ((K)jj[q] << idbits) | (K)(unsigned)x[q], w[q]);
+      }
     }
-    S.ustart[r] = r < R ? lo : U;
-  }
-  __syncthreads();
-  for (int r = tid; r < R; r += kTileThreads)
-    if (S.r_out[r] >= 0) ucount[clo + r] = S.ustart[r + 1] - S.ustart[r];
-  for (int i = tid; i < U; i += kTileThreads) {
-    const K k = sk[padk<K>(i)];
-    const int r = KT::row(k);
-    const int w = hash_get<K>(S.hk, S.hw, hmask, shift, k);
-    stage[S.r_out[r] + (i - S.ustart[r])] = make_int2((int)KT::id(k), w);
+    __syncwarp();
+    const int n = S.ctr;
+    const int rowbits = nnz > 1 ? 32 - __clz(nnz - 1) : 0;
+    block_radix_sort<K, 32, kTinyItems>(S.work, S.sc, n, rowbits + idbits);
+    // ---- runs of equal keys: per sorted row, its first run's index and its
+    // number of runs; then every run to the row's stage
+    unsigned hm[kTinyItems];
+    int qbase = 0;
+#pragma unroll
+    for (int r = 0; r < kTinyItems; ++r) {
+      const int i = r * 32 + lane;
+      const K key = i < n ? S.work[i].k : (K)0;
+      const bool head = i < n && (i == 0 || S.work[i - 1].k != key);
+      hm[r] = __ballot_sync(0xffffffffu, head);
+      if (head) {
+        const int j = (int)(key >> idbits);
+        const int q = qbase + __popc(hm[r] & below);
+        if (i == 0 || (int)(S.work[i - 1].k >> idbits) != j) S.rfirst[j] = q;
+        atomicAdd(&S.rcount[j], 1);
+      }
+      qbase += __popc(hm[r]);
+    }
+    __syncwarp();
+    if (lane < nnz) {
+      const int c = clo + (int)S.nz_row[lane];
+      S.rdst[lane] = eoff[c];
+      ucount[c] = S.rcount[lane];
+    }
+    __syncwarp();
+    qbase = 0;
+#pragma unroll
+    for (int r = 0; r < kTinyItems; ++r) {
+      const int i = r * 32 + lane;
+      if (hm[r] >> lane & 1u) {
+        const K key = S.work[i].k;
+        unsigned sum = (unsigned)S.work[i].v;
+        for (int j2 = i + 1; j2 < n && S.work[j2].k == key; ++j2) sum += (unsigned)S.work[j2].v;
+        const int j = (int)(key >> idbits);
+        const int q = qbase + __popc(hm[r] & below);
+        stage[S.rdst[j] + (q - S.rfirst[j])] = make_int2((int)((unsigned)key & idmask), (int)sum);
+      }
+      qbase += __popc(hm[r]);
+    }
+    __syncwarp();
   }
 }
 
@@ -398,206 +496,38 @@ k_count_scan(const int *__restrict__ ucount, const int *d_cn, int *__restrict__ 
   }
 }
 
-// Copies the short rows' unique entries from the stage to their final place
-// cxadj[c]: one block per group of kCopyGroup consecutive tiles, one thread
-// per entry.
-#ifndef CM_COPY_GROUP
-#define CM_COPY_GROUP 1
-#endif
-#ifndef CM_COPY_THREADS
-#define CM_COPY_THREADS 128
-#endif
-constexpr int kCopyThreads = CM_COPY_THREADS, kCopyGroup = CM_COPY_GROUP;
-constexpr int kCopyBatch = 4;  // stage loads in flight per thread before their stores
-constexpr int kCopyRows = kTileDiag * kCopyGroup;
+// Moves every row of at most kChunk expanded entries from the stage
+// (stage[eoff[c] ..], ucount[c] entries) to its final place cxadj[c]: one warp
+// per row, kCopyBatch loads in flight per lane.
+constexpr int kCopyThreads = 256;
 __global__ void __launch_bounds__(kCopyThreads)
-k_copy_tiles(const int *__restrict__ eoff, const int *d_cn, const int *__restrict__ first_row,
-             const int *__restrict__ ucount, const int *__restrict__ cxadj, const int2 *__restrict__ stage,
-             int *__restrict__ cadjncy, int *__restrict__ cadjwgt) {
-  __shared__ int s_pre[kCopyRows + 1], s_src[kCopyRows], s_dst[kCopyRows], s_scan[kCopyThreads / 32 + 1];
-  const int tid = threadIdx.x;
+k_copy_rows(const int *d_cn, const int *__restrict__ eoff, const int *__restrict__ ucount,
+            const int *__restrict__ cxadj, const int2 *__restrict__ stage, int *__restrict__ cadjncy,
+            int *__restrict__ cadjwgt) {
+  const int lane = threadIdx.x & 31;
   const int nc = *d_cn;
-  const long long dend = (long long)nc + eoff[nc];
-  const long long last = dend / kTileDiag;
-  const long long t0 = (long long)blockIdx.x * kCopyGroup, t1 = t0 + kCopyGroup;
-  const int clo = t0 <= last ? first_row[t0] : nc;
-  const int chi = t1 <= last ? first_row[t1] : nc;
-  const int R = max(0, min(kCopyRows, chi - clo));
-  if (R == 0) return;  // tiles inside a long row's diagonal span
-  constexpr int kRowsPerThread = (kCopyRows + kCopyThreads - 1) / kCopyThreads;
-  int cnt[kRowsPerThread];
-  int mysum = 0;
+  const long long warps = (long long)gridDim.x * (kCopyThreads / 32);
+  for (long long c = (long long)blockIdx.x * (kCopyThreads / 32) + (threadIdx.x >> 5); c < nc; c += warps) {
+    const int e0 = eoff[c];
+    if (eoff[c + 1] - e0 > kChunk) continue;  // chunked: its own copy
+    const int cnt = ucount[c];
+    const int dst = cxadj[c];
+    for (int k0 = lane; k0 < cnt; k0 += 32 * kCopyBatch) {
+      int2 e[kCopyBatch];
 #pragma unroll
-  for (int i = 0; i < kRowsPerThread; ++i) {
-    const int r = tid * kRowsPerThread + i;
-    cnt[i] = 0;
-    if (r < R) {
-      const int c = clo + r;
-      const int e0 = eoff[c];
-      if (eoff[c + 1] - e0 <= kLongThr) cnt[i] = ucount[c];
-      s_src[r] = e0;
-      s_dst[r] = cxadj[c];
-    }
-    mysum += cnt[i];
-  }
-  int U;
-  int ex = block_exclusive_scan<kCopyThreads>(mysum, s_scan, &U);
+      for (int q = 0; q < kCopyBatch; ++q) {
+        const int k = k0 + 32 * q;
+        e[q] = k < cnt ? __ldcs(stage + e0 + k) : make_int2(0, 0);
+      }
 #pragma unroll
-  for (int i = 0; i < kRowsPerThread; ++i) {
-    const int r = tid * kRowsPerThread + i;
-    if (r < R) s_pre[r] = ex;
-    ex += cnt[i];
-  }
-  __syncthreads();
-  for (int o0 = tid; o0 < U; o0 += kCopyBatch * kCopyThreads) {
-    int2 e[kCopyBatch];
-    int d[kCopyBatch];
-#pragma unroll
-    for (int u = 0; u < kCopyBatch; ++u) {
-      const int o = o0 + u * kCopyThreads;
-      d[u] = -1;
-      e[u] = make_int2(0, 0);
-      if (o < U) {
-        const int r = upper_bound_smem(s_pre, R, o) - 1;
-        const int k = o - s_pre[r];
-        e[u] = __ldcs(stage + s_src[r] + k);
-        d[u] = s_dst[r] + k;
+      for (int q = 0; q < kCopyBatch; ++q) {
+        const int k = k0 + 32 * q;
+        if (k < cnt) {
+          cadjncy[dst + k] = e[q].x;
+          cadjwgt[dst + k] = e[q].y;
+        }
       }
     }
-#pragma unroll
-    for (int u = 0; u < kCopyBatch; ++u)
-      if (d[u] >= 0) {
-        cadjncy[d[u]] = e[u].x;
-        cadjwgt[d[u]] = e[u].y;
-      }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Long rows
-// ---------------------------------------------------------------------------
-// Passes a row of length L needs before its chunks form one sorted run.
-__host__ __device__ __forceinline__ int merge_passes(int L) {
-  int p = 0;
-  long long w = kChunk;
-  while (w < L) { w <<= 1; ++p; }
-  return p;
-}
-
-// Chunked rows carry packed entries (coarse id << 32 | weight) through the
-// merge passes.  Pad entries have the id kPadId, above every coarse id
-// (< 2^31 - 1), so they sort to the end of every merged run.
-constexpr unsigned kPadId = 0x7fffffffu;
-__device__ __forceinline__ unsigned long long pack_entry(int2 e) {
-  return ((unsigned long long)(unsigned)e.x << 32) | (unsigned)e.y;
-}
-__device__ __forceinline__ int2 unpack_entry(unsigned long long v) {
-  return make_int2((int)(unsigned)(v >> 32), (int)(unsigned)v);
-}
-
-// Shared memory of one block that merges and sorts up to CAP entries.
-template <int CAP>
-struct MidSmem {
-  unsigned keys[2][padded_k<unsigned>(CAP + 8)];
-  unsigned hk[2 * CAP];
-  int hw[2 * CAP];
-  int ctr;
-};
-
-// Gathers entries [cs, cs + cnt) of coarse row c's expanded row (metadata
-// md), merges duplicates in a shared-memory hash set that sums the weights
-// (self loops dropped), sorts the unique coarse ids (register runs, then
-// merge passes) and writes them with their weights to dst[0 .. U).  Returns U.
-// All NT threads call it; cnt <= CAP.
-template <int NT, int CAP>
-__device__ int unique_sorted_segment(MidSmem<CAP> &S, int c, const int4 &md, int cs, int cnt,
-                                     const int *__restrict__ adjncy, const int *__restrict__ adjwgt,
-                                     const int *__restrict__ cmap, int2 *__restrict__ dst) {
-  constexpr int kLg = ilog2(2 * CAP);
-  const int lg = hash_log2(cnt, kLg);
-  const int hsize = 1 << lg, shift = 64 - lg;
-  const unsigned hmask = hsize - 1;
-  if (threadIdx.x == 0) S.ctr = 0;
-  for (int t = threadIdx.x; t < hsize; t += NT) {
-    S.hk[t] = ~0u;
-    S.hw[t] = 0;
-  }
-  __syncthreads();
-  for (int t0 = threadIdx.x; t0 < cnt; t0 += 4 * NT) {
-    int src[4], x[4], w[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int t = t0 + u * NT;
-      src[u] = t < cnt ? expanded_src(cs + t, md.x, md.y, md.z) : -1;
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      x[u] = src[u] >= 0 ? adjncy[src[u]] : 0;
-      w[u] = src[u] >= 0 ? adjwgt[src[u]] : 0;
-    }
-#pragma unroll
-    for (int u = 0; u < 4; ++u) x[u] = src[u] >= 0 ? cmap[x[u]] : 0;
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-      if (src[u] >= 0 && x[u] != c) hash_add<unsigned>(S.hk, S.hw, hmask, shift, (unsigned)x[u], w[u]);
-  }
-  __syncthreads();
-  const int U = hash_compact<unsigned, NT>(S.hk, hsize, S.keys[0], &S.ctr);
-  const int b = block_sort_keys<unsigned, NT, 8>(S.keys[0], S.keys[1], U);
-  const unsigned *sk = S.keys[b];
-  for (int t = threadIdx.x; t < U; t += NT) {
-    const unsigned k = sk[padk<unsigned>(t)];
-    dst[t] = make_int2((int)k, hash_get<unsigned>(S.hk, S.hw, hmask, shift, k));
-  }
-  return U;
-}
-
-// Rows too long for a tile but <= kChunk entries, one size class per launch:
-// one block per row writes the row's unique entries to stage[eoff[c] ...) and
-// their number to ucount[c].
-template <int NT, int CAP>
-__global__ void __launch_bounds__(NT)
-k_mid_rows(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
-           const int *__restrict__ eoff, const int4 *__restrict__ row_meta, const int *__restrict__ list,
-           const int *__restrict__ count, int2 *__restrict__ stage, int *__restrict__ ucount) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  MidSmem<CAP> &S = *reinterpret_cast<MidSmem<CAP> *>(smem_raw);
-  const int nrows = *count;
-  for (int i = blockIdx.x; i < nrows; i += gridDim.x) {
-    const int c = list[i];
-    const int4 md = row_meta[c];
-    const int U = unique_sorted_segment<NT, CAP>(S, c, md, 0, min(md.w, CAP), adjncy, adjwgt, cmap, stage + eoff[c]);
-    if (threadIdx.x == 0) ucount[c] = U;
-    __syncthreads();
-  }
-}
-
-// Rows longer than kChunk: each chunk of kChunk entries becomes one sorted run
-// in stage0 for the merge passes -- its unique entries (duplicates within the
-// chunk already merged, self loops dropped), then pad entries up to the
-// chunk's length, which sort after every coarse id and are skipped by the
-// dedup.  chunk_np[q] = the merge passes the chunk's row needs.
-__global__ void __launch_bounds__(kChunkThreads, 1)
-k_long_sort(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
-            const int *__restrict__ eoff, const int4 *__restrict__ row_meta, const int *__restrict__ long_list,
-            const int *__restrict__ chunk_row, const unsigned long long *long_ctr, int2 *__restrict__ stage,
-            int *__restrict__ ucount, int *__restrict__ chunk_np) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  MidSmem<kChunk> &S = *reinterpret_cast<MidSmem<kChunk> *>(smem_raw);
-  const int nchunks = (int)(*long_ctr & 0xffffffffu);
-  for (int q = blockIdx.x; q < nchunks; q += gridDim.x) {
-    const int idx = chunk_row[q];
-    const int c = long_list[2 * idx];
-    const int4 md = row_meta[c];
-    const int j = q - long_list[2 * idx + 1];
-    const int cs = j * kChunk;
-    const int cnt = min(kChunk, md.w - cs);
-    if (j == 0 && threadIdx.x == 0) ucount[c] = 0;  // the dedup adds the chunks' counts
-    if (threadIdx.x == 0) chunk_np[q] = merge_passes(md.w);
-    int2 *dst = stage + eoff[c] + cs;
-    const int U = unique_sorted_segment<kChunkThreads, kChunk>(S, c, md, cs, cnt, adjncy, adjwgt, cmap, dst);
-    for (int t = U + threadIdx.x; t < cnt; t += kChunkThreads) dst[t] = make_int2((int)kPadId, 0);
-    __syncthreads();
   }
 }
 
@@ -661,7 +591,7 @@ struct MergeSmem {
 __global__ void __launch_bounds__(kMergeThreads, kMergeBlocksPerSm)
 k_long_merge(int p, const int *__restrict__ long_list, const int *__restrict__ chunk_row, const int *__restrict__ eoff,
              const unsigned long long *long_ctr, const int *__restrict__ chunk_np, int2 *stage0, int2 *stage1,
-             const DevStatus *st) {
+             DevStatus *st) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MergeSmem &S = *reinterpret_cast<MergeSmem *>(smem_raw);
   if (p >= merge_passes(st->max_row)) return;
@@ -703,6 +633,12 @@ k_long_merge(int p, const int *__restrict__ long_list, const int *__restrict__ c
       const int i0 = S.cut[0], i1 = S.cut[1];
       const int na = i1 - i0, nb = nout - na;
       const int j0 = d0 - i0;
+      if (na < 0 || nb < 0 || i1 > alen || j0 + nb > blen) {
+        // cuts of runs that are not sorted: report, read nothing
+        if (threadIdx.x == 0) record_error(st, CM_ERR_INVALID, ERR_SITE_BOUNDS);
+        __syncthreads();
+        continue;
+      }
       // window: A[i0 .. i1) then B[j0 .. j0 + nb)
       {
         int2 e[kMergePer];
@@ -819,49 +755,31 @@ k_long_dedup(const int *__restrict__ long_list, const int *__restrict__ chunk_ro
   }
 }
 
-// Copies every long row's unique entries to its final place once cxadj is
-// known: first the size-class rows (stage1 at eoff[c]), then the chunks of the
-// chunked rows (each at cxadj[c] + the unique entries of the row's earlier
-// chunks).
+// Copies the chunked rows' unique entries to their final place once cxadj is
+// known: each chunk at cxadj[c] + the unique entries of the row's earlier
+// chunks.
 __global__ void k_long_copy(const int *__restrict__ long_list, const int *__restrict__ chunk_row,
-                            const int *__restrict__ eoff, const unsigned long long *long_ctr,
-                            const int *__restrict__ mid_list, const int *__restrict__ mid_ctr, int mid_cap,
-                            const int2 *stage0, const int2 *stage1, const int *__restrict__ chunk_cnt,
-                            const int *__restrict__ ucount, const int *__restrict__ cxadj, int *__restrict__ cadjncy,
-                            int *__restrict__ cadjwgt) {
+                            const int *__restrict__ eoff, const unsigned long long *long_ctr, const int2 *stage0,
+                            const int2 *stage1, const int *__restrict__ chunk_cnt, const int *__restrict__ cxadj,
+                            int *__restrict__ cadjncy, int *__restrict__ cadjwgt) {
   __shared__ int s_pre[32];
-  const int n0 = mid_ctr[0], n1 = mid_ctr[1], n2 = mid_ctr[2];
-  const int nmid = n0 + n1 + n2;
   const int nchunks = (int)(*long_ctr & 0xffffffffu);
-  for (int q = blockIdx.x; q < nmid + nchunks; q += gridDim.x) {
-    int cnt;
-    long long dst;
-    const int2 *src;
-    if (q < nmid) {
-      const int cls = q < n0 ? 0 : (q < n0 + n1 ? 1 : 2);
-      const int i = q - (cls == 0 ? 0 : (cls == 1 ? n0 : n0 + n1));
-      const int c = mid_list[(size_t)cls * mid_cap + i];
-      src = stage1 + eoff[c];
-      cnt = ucount[c];
-      dst = cxadj[c];
-    } else {
-      const int qq = q - nmid;
-      const int idx = chunk_row[qq];
-      const int c = long_list[2 * idx];
-      const int first = long_list[2 * idx + 1];
-      const int L = eoff[c + 1] - eoff[c];
-      src = ((merge_passes(L) & 1) ? stage0 : stage1) + eoff[c] + (long long)(qq - first) * kChunk;
-      cnt = chunk_cnt[qq];
-      int pre = 0;
-      for (int k = first + threadIdx.x; k < qq; k += blockDim.x) pre += chunk_cnt[k];
-      pre = __reduce_add_sync(0xffffffffu, pre);
-      if ((threadIdx.x & 31) == 0) s_pre[threadIdx.x >> 5] = pre;
-      __syncthreads();
-      pre = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) pre += s_pre[w];
-      __syncthreads();
-      dst = (long long)cxadj[c] + pre;
-    }
+  for (int q = blockIdx.x; q < nchunks; q += gridDim.x) {
+    const int idx = chunk_row[q];
+    const int c = long_list[2 * idx];
+    const int first = long_list[2 * idx + 1];
+    const int L = eoff[c + 1] - eoff[c];
+    const int2 *src = ((merge_passes(L) & 1) ? stage0 : stage1) + eoff[c] + (long long)(q - first) * kChunk;
+    const int cnt = chunk_cnt[q];
+    int pre = 0;
+    for (int k = first + threadIdx.x; k < q; k += blockDim.x) pre += chunk_cnt[k];
+    pre = __reduce_add_sync(0xffffffffu, pre);
+    if ((threadIdx.x & 31) == 0) s_pre[threadIdx.x >> 5] = pre;
+    __syncthreads();
+    pre = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) pre += s_pre[w];
+    __syncthreads();
+    const long long dst = (long long)cxadj[c] + pre;
     for (int t0 = threadIdx.x; t0 < cnt; t0 += kCopyBatch * blockDim.x) {
       int2 e[kCopyBatch];
 #pragma unroll
@@ -887,19 +805,55 @@ __global__ void k_long_copy(const int *__restrict__ long_list, const int *__rest
 // than items (at least one), at most `cap`.
 static unsigned grid_for(int64_t cap, int64_t items) { return (unsigned)std::max<int64_t>(1, std::min(cap, items)); }
 
+namespace {
+// Tiny units of a graph of n vertices and m entries: at most (n + m) / D + 1.
+int64_t units_max(int64_t n, int64_t m) { return (n + m) / kTinyDiag + 2; }
+int64_t class_list_size(int64_t m) { return class_offset(m, kTinyMax, kRowClasses); }
+
+template <int K>
+void class_attrs(cm_ctx *ctx) {
+  constexpr int NT = class_threads(K), IT = class_items(K);
+  cudaFuncSetAttribute(k_class_rows<NT, IT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SegSmem<NT, IT>));
+  int b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_class_rows<NT, IT>, NT, sizeof(SegSmem<NT, IT>));
+  ctx->class_blocks_per_sm[K] = std::max(1, b);
+  if constexpr (K + 1 < kClasses) class_attrs<K + 1>(ctx);
+}
+
+// Launches the class kernels of the classes a row of at most row_bound
+// entries can fall in, round-robin on the auxiliary streams.
+template <int K>
+void launch_classes(cm_ctx *ctx, const cm_graph *fine, const int *cmap, const int *eoff, const int4 *row_meta,
+                    const int *class_list, const int *class_ctr, const int *d_sizes, int2 *stage, int *ucount,
+                    int64_t row_bound) {
+  constexpr int NT = class_threads(K), IT = class_items(K);
+  const int64_t m = fine->nedges;
+  if (row_bound > ((int64_t)kTinyMax << K)) {
+    const unsigned grid = grid_for((int64_t)ctx->num_sms * ctx->class_blocks_per_sm[K], class_cap(m, kTinyMax, K));
+    k_class_rows<NT, IT><<<grid, NT, sizeof(SegSmem<NT, IT>), ctx->aux[K % cm_ctx::kAux]>>>(
+        fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, class_list + class_offset(m, kTinyMax, K), class_ctr + K,
+        d_sizes, stage, ucount);
+    ctx->launches++;
+  }
+  if constexpr (K + 1 < kClasses)
+    launch_classes<K + 1>(ctx, fine, cmap, eoff, row_meta, class_list, class_ctr, d_sizes, stage, ucount, row_bound);
+}
+}  // namespace
+
 size_t contract_ws_bytes(int64_t n, int64_t m) {
-  const int64_t ntiles = (n + m) / kTileDiag + 2;
-  const int64_t nchunks = m / kChunk + m / kLongThr + 2;
+  const int64_t nunits = units_max(n, m);
+  const int64_t nchunks = m / kChunk + 2;
   size_t b = 0;
-  b += (size_t)n * 4 * 3 + 4 * 256;          // leader, ucount, eoff(+1)
-  b += (size_t)(ntiles + 2) * 4 + 256;       // first_row
-  b += (size_t)(m / kChunk + 2) * 8 + 256;   // long_list
-  b += (size_t)(m / (kLongThr + 1) + 2) * 12 + 256;  // size-class lists
-  b += (size_t)nchunks * 4 * 3 + 768;        // chunk_row, chunk_cnt, chunk_np
-  b += 256;                                  // counters
-  b += (size_t)(ntiles + 2) * 8 + 256;       // tile look-back
-  b += (size_t)n * 16 + 256;                 // row metadata
-  b += (size_t)m * 8 * 2 + 512;              // stages
+  b += (size_t)n * 4 * 3 + 4 * 256;                    // leader, ucount, eoff(+1)
+  b += (size_t)(nunits + 2) * 4 + 256;                 // first row of every tiny unit
+  b += (size_t)(m / kChunk + 2) * 8 + 256;             // long_list
+  b += (size_t)class_list_size(m) * 4 + 256;           // class lists
+  b += (size_t)nchunks * 4 * 3 + 768;                  // chunk_row, chunk_cnt, chunk_np
+  b += 256;                                            // counters
+  b += (size_t)(n / kMapTile + 3) * 8 + 256;           // unit-map look-back
+  b += (size_t)(n / (kScanThreads * kScanItems) + 3) * 8 + 256;  // count-scan look-back
+  b += (size_t)n * 16 + 256;                           // row metadata
+  b += (size_t)m * 8 * 2 + 512;                        // stages
   b += cmap_ws_bytes(n);
   return b + 4096;
 }
@@ -912,90 +866,84 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
     cudaMemsetAsync(coarse->xadj, 0, sizeof(int32_t), s);
     return cuda_status(cudaGetLastError(), "contract(empty)");
   }
-  const int64_t ntiles = (n + m) / kTileDiag + 1;
-  const int64_t nchunks_max = m / kChunk + m / kLongThr + 2;
-  const int64_t mid_cap = m / (kLongThr + 1) + 2;
-  int *leader = (int *)ws_take(ctx, (size_t)n * 4);
-  int *ucount = (int *)ws_take(ctx, (size_t)n * 4);
-  int *eoff = (int *)ws_take(ctx, (size_t)(n + 1) * 4);
-  int *first_row = (int *)ws_take(ctx, (size_t)(ntiles + 2) * 4);
-  int *long_list = (int *)ws_take(ctx, (size_t)(m / kChunk + 2) * 8);
-  int *chunk_row = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
-  int *chunk_cnt = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
-  int *chunk_np = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
-  int *mid_list = (int *)ws_take(ctx, (size_t)mid_cap * 3 * 4);
-  int4 *row_meta = (int4 *)ws_take(ctx, (size_t)n * 16);
-  unsigned long long *ctr = (unsigned long long *)ws_take(ctx, 64);   // [0] chunked rows, [1] mid counters
-  unsigned long long *lb = (unsigned long long *)ws_take(ctx, (size_t)(ntiles + 2) * 8);
-  int2 *stage0 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
-  int2 *stage1 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
-  if (!leader || !ucount || !eoff || !first_row || !long_list || !chunk_row || !chunk_cnt || !chunk_np || !mid_list ||
-      !row_meta || !ctr || !lb ||
-      !stage0 || !stage1)
-    return cm_fail(CM_ERR_NOMEM, "contract: workspace too small");
-  int *mid_ctr = reinterpret_cast<int *>(ctr + 1);
-  DevStatus *st = ctx->d_status;
-  cudaMemsetAsync(ctr, 0, 64, s);
-  cudaMemsetAsync(&st->max_row, 0, sizeof(int), s);
-  cudaMemsetAsync(lb, 0, (size_t)(n / (kScanThreads * kScanItems) + 3) * 8, s);
-  int rc = launch_cmap(ctx, (int32_t)n, fine->xadj, fine->vwgt, match, cmap, leader, coarse->vwgt, eoff,
-                       d_sizes /* n' lands in d_sizes[0] */, long_list, kLongThr, kChunk, ctr, chunk_row, first_row,
-                       kTileDiag, mid_list, mid_ctr, (int32_t)mid_cap, row_meta, s);
-  if (rc) return rc;
-  const int sms = ctx->num_sms;
-  const bool small_ids = n <= kSmallIdMaxN;
-  const size_t tile_smem = small_ids ? sizeof(TileSmem<unsigned>) : sizeof(TileSmem<unsigned long long>);
   if (!ctx->contract_attrs_set) {  // once per context (the attributes last for the process)
-    cudaFuncSetAttribute(k_contract_tiles<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sizeof(TileSmem<unsigned>));
-    cudaFuncSetAttribute(k_contract_tiles<unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sizeof(TileSmem<unsigned long long>));
-    cudaFuncSetAttribute(k_mid_rows<kMidThreads0, 2 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sizeof(MidSmem<2 * kLongThr>));
-    cudaFuncSetAttribute(k_mid_rows<kMidThreads1, 4 * kLongThr>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sizeof(MidSmem<4 * kLongThr>));
-    cudaFuncSetAttribute(k_mid_rows<1024, kChunk>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sizeof(MidSmem<kChunk>));
-    cudaFuncSetAttribute(k_long_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MidSmem<kChunk>));
+    cudaFuncSetAttribute(k_tiny_units<unsigned>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(TinySmem<unsigned>));
+    cudaFuncSetAttribute(k_tiny_units<unsigned long long>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(TinySmem<unsigned long long>));
+    cudaFuncSetAttribute(k_long_sort, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sizeof(SegSmem<kChunkThreads, kChunkItems>));
     cudaFuncSetAttribute(k_long_merge, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MergeSmem));
+    class_attrs<0>(ctx);
+    int b32 = 0, b64 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b32, k_tiny_units<unsigned>, 32, sizeof(TinySmem<unsigned>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b64, k_tiny_units<unsigned long long>, 32,
+                                                  sizeof(TinySmem<unsigned long long>));
+    ctx->unit_blocks_per_sm[0] = std::max(1, b32);
+    ctx->unit_blocks_per_sm[1] = std::max(1, b64);
     if (int rc2 = check_launch(ctx, "contract: kernel attributes")) return rc2;
     ctx->contract_attrs_set = true;
   }
+  const int64_t nunits = units_max(n, m);
+  const int64_t nchunks_max = m / kChunk + 2;
+  const int64_t map_tiles = (n + kMapTile - 1) / kMapTile;
+  const int64_t scan_tiles = (n + kScanThreads * kScanItems - 1) / (kScanThreads * kScanItems);
+  int *leader = (int *)ws_take(ctx, (size_t)n * 4);
+  int *ucount = (int *)ws_take(ctx, (size_t)n * 4);
+  int *eoff = (int *)ws_take(ctx, (size_t)(n + 1) * 4);
+  int *first_row = (int *)ws_take(ctx, (size_t)(nunits + 2) * 4);
+  int *long_list = (int *)ws_take(ctx, (size_t)(m / kChunk + 2) * 8);
+  int *class_list = (int *)ws_take(ctx, (size_t)class_list_size(m) * 4);
+  int *chunk_row = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
+  int *chunk_cnt = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
+  int *chunk_np = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
+  int4 *row_meta = (int4 *)ws_take(ctx, (size_t)n * 16);
+  // [0] chunked rows (rows << 32 | chunks); ints 2..9 the class counters;
+  // int 12 the last tiny unit's index
+  unsigned long long *ctr = (unsigned long long *)ws_take(ctx, 64);
+  unsigned long long *map_lb = (unsigned long long *)ws_take(ctx, (size_t)(map_tiles + 3) * 8);
+  unsigned long long *scan_lb = (unsigned long long *)ws_take(ctx, (size_t)(scan_tiles + 3) * 8);
+  int2 *stage0 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
+  int2 *stage1 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
+  if (!leader || !ucount || !eoff || !first_row || !long_list || !class_list || !chunk_row || !chunk_cnt ||
+      !chunk_np || !row_meta || !ctr || !map_lb || !scan_lb || !stage0 || !stage1)
+    return cm_fail(CM_ERR_NOMEM, "contract: workspace too small");
+  int *class_ctr = reinterpret_cast<int *>(ctr) + 2;
+  int *unit_last = reinterpret_cast<int *>(ctr) + 12;
+  DevStatus *st = ctx->d_status;
+  cudaMemsetAsync(ctr, 0, 64, s);
+  cudaMemsetAsync(&st->max_row, 0, sizeof(int), s);
+  cudaMemsetAsync(map_lb, 0, (size_t)(map_tiles + 3) * 8, s);
+  cudaMemsetAsync(scan_lb, 0, (size_t)(scan_tiles + 3) * 8, s);
+  int rc = launch_cmap(ctx, (int32_t)n, fine->xadj, fine->vwgt, match, cmap, leader, coarse->vwgt, eoff,
+                       d_sizes /* n' lands in d_sizes[0] */, long_list, kTinyMax, kChunk, ctr, chunk_row, class_list,
+                       class_ctr, m, row_meta, s);
+  if (rc) return rc;
+  const int sms = ctx->num_sms;
+  const bool small_ids = n <= (1ll << (32 - kTinyRowBits));
 
-  // Long rows on the auxiliary streams (three size classes; the chunked
-  // rows' sort, merge passes and dedup after the largest class) while the
-  // tiles do the short rows on the caller's stream.  All of them leave their
-  // unique entries in stage1 at eoff[c] (the chunked rows in the stage their
-  // merge parity picks) and their number in ucount[c].  Classes above
-  // row_bound (an upper bound of the expanded row length known to the
-  // caller) cannot have rows and are not launched.
-  const bool any_long = row_bound > kLongThr;
-  const bool class1 = row_bound > 2 * kLongThr, class2 = row_bound > 4 * kLongThr, chunked = row_bound > kChunk;
+  // Rows above kTinyMax on the auxiliary streams (one kernel per size class;
+  // the chunked rows' sort, merge passes and dedup on the last stream), the
+  // tiny units on the caller's stream; every row's unique entries land in
+  // stage1 at eoff[c] (the chunked rows in the stage their merge parity
+  // picks) and their number in ucount[c].  Classes above row_bound (an upper
+  // bound of the expanded row length known to the caller) cannot have rows
+  // and are not launched.
+  const bool any_big = row_bound > kTinyMax;
+  const bool chunked = row_bound > kChunk;
   stage_begin(ctx, s);
-  if (any_long) {
+  if (any_big) {
     cudaEventRecord(ctx->fork_ev, s);
-    for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(ctx->aux[i], ctx->fork_ev, 0);
-    k_mid_rows<kMidThreads0, 2 * kLongThr><<<grid_for(sms * 4, m / (kLongThr + 1)), kMidThreads0,
-                                             sizeof(MidSmem<2 * kLongThr>), ctx->aux[0]>>>(
-        fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list, mid_ctr + 0, stage1, ucount);
-    ctx->launches++;
-    if (class1) {
-      k_mid_rows<kMidThreads1, 4 * kLongThr><<<grid_for(sms * 2, m / (2 * kLongThr + 1)), kMidThreads1,
-                                               sizeof(MidSmem<4 * kLongThr>), ctx->aux[1]>>>(
-          fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + mid_cap, mid_ctr + 1, stage1, ucount);
-      ctx->launches++;
-    }
-    if (class2) {
-      k_mid_rows<1024, kChunk><<<grid_for(sms, m / (4 * kLongThr + 1)), 1024, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
-          fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, mid_list + 2 * mid_cap, mid_ctr + 2, stage1, ucount);
-      ctx->launches++;
-    }
+    for (int i = 0; i < cm_ctx::kAux; ++i) cudaStreamWaitEvent(ctx->aux[i], ctx->fork_ev, 0);
+    launch_classes<0>(ctx, fine, cmap, eoff, row_meta, class_list, class_ctr, d_sizes, stage1, ucount, row_bound);
     if (chunked) {
+      cudaStream_t cs = ctx->aux[cm_ctx::kAux - 1];
       // Grids of the chunked-row kernels scale with the most chunks the graph
       // can have (m / kChunk), so small graphs do not claim every SM.
       const int long_grid = (int)std::min<int64_t>(sms, m / kChunk / 4 + 1);
-      k_long_sort<<<long_grid, kChunkThreads, sizeof(MidSmem<kChunk>), ctx->aux[2]>>>(
-          fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, long_list, chunk_row, ctr, stage0, ucount, chunk_np);
+      k_long_sort<<<long_grid, kChunkThreads, sizeof(SegSmem<kChunkThreads, kChunkItems>), cs>>>(
+          fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, long_list, chunk_row, ctr, d_sizes, stage0, ucount,
+          chunk_np);
       ctx->launches++;
       // Passes a row of at most min(m, row_bound) entries can need; each is a
       // plain launch.
@@ -1003,50 +951,54 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
       for (int64_t w = kChunk; w < std::min<int64_t>(m, row_bound); w <<= 1) ++max_pass;
       const int merge_grid = (int)std::min<int64_t>((int64_t)sms * kMergeBlocksPerSm, m / kMergeOut + 1);
       for (int p = 0; p < max_pass; ++p) {
-        k_long_merge<<<merge_grid, kMergeThreads, sizeof(MergeSmem), ctx->aux[2]>>>(p, long_list, chunk_row, eoff, ctr,
-                                                                                    chunk_np, stage0, stage1, st);
+        k_long_merge<<<merge_grid, kMergeThreads, sizeof(MergeSmem), cs>>>(p, long_list, chunk_row, eoff, ctr,
+                                                                          chunk_np, stage0, stage1, st);
         ctx->launches++;
       }
-      k_long_dedup<<<long_grid * 4, kDedupThreads, 0, ctx->aux[2]>>>(long_list, chunk_row, eoff, ctr, stage0, stage1,
-                                                                     stage0, stage1, chunk_cnt, ucount);
+      k_long_dedup<<<long_grid * 4, kDedupThreads, 0, cs>>>(long_list, chunk_row, eoff, ctr, stage0, stage1, stage0,
+                                                            stage1, chunk_cnt, ucount);
       ctx->launches++;
     }
-    for (int i = 0; i < 3; ++i) cudaEventRecord(ctx->join_ev[i], ctx->aux[i]);
   }
-  // d_sizes[0] holds n' (written by the cmap scan).
-  if (small_ids)
-    k_contract_tiles<unsigned><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
-        fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, stage1, ucount, st);
-  else
-    k_contract_tiles<unsigned long long><<<(unsigned)ntiles, kTileThreads, tile_smem, s>>>(
-        fine->adjncy, fine->adjwgt, cmap, eoff, d_sizes, first_row, row_meta, stage1, ucount, st);
+  k_unit_map<<<(unsigned)std::max<int64_t>(1, map_tiles), kMapThreads, 0, s>>>(d_sizes, eoff, first_row, unit_last,
+                                                                                map_lb, st);
   ctx->launches++;
-  if (any_long)
-    for (int i = 0; i < 3; ++i) cudaStreamWaitEvent(s, ctx->join_ev[i], 0);
-  stage_end(ctx, CM_STAGE_TILES, s);
+  const unsigned tiny_grid = grid_for((int64_t)sms * ctx->unit_blocks_per_sm[small_ids ? 0 : 1], nunits);
+  if (small_ids)
+    k_tiny_units<unsigned><<<tiny_grid, 32, sizeof(TinySmem<unsigned>), s>>>(
+        fine->adjncy, fine->adjwgt, cmap, d_sizes, first_row, unit_last, row_meta, eoff, stage1, ucount, st);
+  else
+    k_tiny_units<unsigned long long><<<tiny_grid, 32, sizeof(TinySmem<unsigned long long>), s>>>(
+        fine->adjncy, fine->adjwgt, cmap, d_sizes, first_row, unit_last, row_meta, eoff, stage1, ucount, st);
+  ctx->launches++;
+  if (any_big)
+    for (int i = 0; i < cm_ctx::kAux; ++i) {
+      cudaEventRecord(ctx->join_ev[i], ctx->aux[i]);
+      cudaStreamWaitEvent(s, ctx->join_ev[i], 0);
+    }
+  stage_end(ctx, CM_STAGE_ROWS, s);
 
   // cxadj = exclusive scan of ucount; d_sizes[1] = m'.
   stage_begin(ctx, s);
-  const int64_t scan_tiles = (n + kScanThreads * kScanItems - 1) / (kScanThreads * kScanItems);
-  k_count_scan<<<(unsigned)scan_tiles, kScanThreads, 0, s>>>(ucount, d_sizes, coarse->xadj, d_sizes, lb, st);
+  k_count_scan<<<(unsigned)std::max<int64_t>(1, scan_tiles), kScanThreads, 0, s>>>(ucount, d_sizes, coarse->xadj,
+                                                                                     d_sizes, scan_lb, st);
   ctx->launches++;
   stage_end(ctx, CM_STAGE_SCAN, s);
 
   // Every row's unique entries to their final place.
   stage_begin(ctx, s);
-  if (any_long) {
+  if (chunked) {
     cudaEventRecord(ctx->fork_ev, s);
     cudaStreamWaitEvent(ctx->aux[0], ctx->fork_ev, 0);
-    k_long_copy<<<grid_for(sms * 4, m / kLongThr), 256, 0, ctx->aux[0]>>>(
-        long_list, chunk_row, eoff, ctr, mid_list, mid_ctr, (int)mid_cap, stage0, stage1, chunk_cnt, ucount,
-        coarse->xadj, coarse->adjncy, coarse->adjwgt);
-    cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
+    k_long_copy<<<grid_for(sms * 4, m / kChunk + 1), 256, 0, ctx->aux[0]>>>(
+        long_list, chunk_row, eoff, ctr, stage0, stage1, chunk_cnt, coarse->xadj, coarse->adjncy, coarse->adjwgt);
     ctx->launches++;
+    cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
   }
-  k_copy_tiles<<<(unsigned)((ntiles + kCopyGroup - 1) / kCopyGroup), kCopyThreads, 0, s>>>(
-      eoff, d_sizes, first_row, ucount, coarse->xadj, stage1, coarse->adjncy, coarse->adjwgt);
+  k_copy_rows<<<grid_for((int64_t)sms * 8, n / (kCopyThreads / 32) + 1), kCopyThreads, 0, s>>>(
+      d_sizes, eoff, ucount, coarse->xadj, stage1, coarse->adjncy, coarse->adjwgt);
   ctx->launches++;
-  if (any_long) cudaStreamWaitEvent(s, ctx->join_ev[0], 0);
+  if (chunked) cudaStreamWaitEvent(s, ctx->join_ev[0], 0);
   stage_end(ctx, CM_STAGE_COPY, s);
   return check_launch(ctx, "contract");
 }

@@ -185,7 +185,7 @@ extern "C" int cm_ctx_create(int device, cm_ctx **out) {
   if (!rc) rc = cuda_status(cudaMallocHost(&ctx->h_status, sizeof(DevStatus)), "pinned status alloc");
   if (!rc) rc = cuda_status(cudaMallocHost(&ctx->h_small, 64), "pinned readback alloc");
   if (!rc) rc = cuda_status(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "context stream");
-  for (int i = 0; i < 3 && !rc; ++i) {
+  for (int i = 0; i < cm_ctx::kAux && !rc; ++i) {
     rc = cuda_status(cudaStreamCreateWithFlags(&ctx->aux[i], cudaStreamNonBlocking), "aux stream");
     if (!rc) rc = cuda_status(cudaEventCreateWithFlags(&ctx->join_ev[i], cudaEventDisableTiming), "aux event");
   }
@@ -225,7 +225,7 @@ extern "C" void cm_ctx_destroy(cm_ctx *ctx) {
   if (ctx->h_status) cudaFreeHost(ctx->h_status);
   if (ctx->h_small) cudaFreeHost(ctx->h_small);
   if (ctx->d_trace) cudaFree(ctx->d_trace);
-  for (int i = 0; i < 3; ++i) {
+  for (int i = 0; i < cm_ctx::kAux; ++i) {
     if (ctx->aux[i]) cudaStreamDestroy(ctx->aux[i]);
     if (ctx->join_ev[i]) cudaEventDestroy(ctx->join_ev[i]);
   }
@@ -316,7 +316,7 @@ extern "C" int cm_ctx_match_trace(cm_ctx *ctx, int64_t *out, int32_t cap_rows, i
 }
 
 extern "C" const char *cm_stage_name(int32_t stage) {
-  static const char *names[CM_STAGE_COUNT] = {"k_match", "k_cmap", "k_contract_tiles", "k_count_scan", "k_copy_tiles"};
+  static const char *names[CM_STAGE_COUNT] = {"k_match", "k_cmap", "k_rows", "k_count_scan", "k_copy_rows"};
   return stage >= 0 && stage < CM_STAGE_COUNT ? names[stage] : "";
 }
 
@@ -357,7 +357,7 @@ extern "C" int cm_build_cmap(cm_ctx *ctx, int32_t nvtxs, const int32_t *d_xadj, 
   ws_reset(ctx);
   if ((rc = ws_ensure(ctx, cmap_ws_bytes(nvtxs)))) return rc;
   return launch_cmap(ctx, nvtxs, d_xadj, d_vwgt, d_match, d_cmap, d_leader, d_cvwgt, d_eoff, d_cnvtxs, nullptr, 0,
-                     1, nullptr, nullptr, nullptr, 0, nullptr, nullptr, 0, nullptr, (cudaStream_t)stream);
+                     1, nullptr, nullptr, nullptr, nullptr, 0, nullptr, (cudaStream_t)stream);
 }
 
 extern "C" int cm_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *d_match, int32_t *d_cmap,

@@ -35,8 +35,9 @@ struct cm_ctx {
   // so contexts running side by side never wait on each other's streams
   cudaMemPool_t pool = nullptr;
   // internal streams/events for concurrent contraction stages
-  cudaStream_t aux[3] = {nullptr, nullptr, nullptr};
-  cudaEvent_t fork_ev = nullptr, join_ev[3] = {nullptr, nullptr, nullptr};
+  static constexpr int kAux = 4;
+  cudaStream_t aux[kAux] = {nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t fork_ev = nullptr, join_ev[kAux] = {nullptr, nullptr, nullptr, nullptr};
   // matching trace (optional): 8 x uint64 per row, row 0 = header
   unsigned long long *d_trace = nullptr;
   int trace_rows = 0;
@@ -48,6 +49,10 @@ struct cm_ctx {
   // the matching kernel's resident blocks per SM (per tie order)
   bool contract_attrs_set = false;
   int match_blocks_per_sm[2] = {0, 0};
+  // resident blocks per SM of the contraction's tiny-unit kernel (32- and
+  // 64-bit keys) and of its row-class kernels
+  int unit_blocks_per_sm[2] = {1, 1};
+  int class_blocks_per_sm[8] = {1, 1, 1, 1, 1, 1, 1, 1};
 };
 
 namespace cm {
@@ -77,6 +82,17 @@ int take_device_error(cm_ctx *ctx, cudaStream_t s);
 int cuda_status(cudaError_t e, const char *what);
 int check_launch(cm_ctx *ctx, const char *what);
 
+// Row classes of the contraction: class k lists the coarse rows of
+// base * 2^k < L <= base * 2^(k+1) expanded entries (L <= the chunk size),
+// at class_offset(m, base, k) of one list array, at most class_cap entries.
+constexpr int kRowClasses = 8;
+__host__ __device__ inline int64_t class_cap(int64_t m, int base, int k) { return m / ((int64_t)base << k) + 2; }
+__host__ __device__ inline int64_t class_offset(int64_t m, int base, int k) {
+  int64_t o = 0;
+  for (int i = 0; i < k; ++i) o += class_cap(m, base, i);
+  return o;
+}
+
 // Workspace bytes each stage needs for a graph of n vertices, m entries.
 size_t match_ws_bytes(int64_t n, int64_t m);
 size_t cmap_ws_bytes(int64_t n);
@@ -85,11 +101,14 @@ size_t contract_ws_bytes(int64_t n, int64_t m);
 // Stage launchers shared between entry points (no argument checking).
 int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, int32_t *d_match,
                  cudaStream_t s);
+// Rows of more than long_threshold expanded entries are listed: up to
+// long_chunk entries by size class (class_offset(m, long_threshold, k) of
+// class_list, counts in class_ctr[k]), longer ones as chunked rows.
 int launch_cmap(cm_ctx *ctx, int32_t n, const int32_t *xadj, const int32_t *vwgt, const int32_t *match,
                 int32_t *cmap, int32_t *leader, int32_t *cvwgt, int32_t *eoff, int32_t *d_cnvtxs,
                 int32_t *long_list, int32_t long_threshold, int32_t long_chunk, unsigned long long *d_long_ctr,
-                int32_t *chunk_row, int32_t *first_row, int32_t tile_diag, int32_t *mid_list, int32_t *mid_ctr,
-                int32_t mid_cap, void *row_meta, cudaStream_t s);
+                int32_t *chunk_row, int32_t *class_list, int32_t *class_ctr, int64_t m, void *row_meta,
+                cudaStream_t s);
 // row_bound: an upper bound of the longest expanded coarse row (INT64_MAX
 // when unknown); kernels of row classes above it are not launched.
 int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int32_t *cmap, cm_graph *coarse,

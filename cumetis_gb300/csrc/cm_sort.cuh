@@ -1,12 +1,20 @@
-// cm_sort.cuh -- block-wide sort of keys in shared memory.
+// cm_sort.cuh -- shared-memory sorting helpers of the contraction.
 //
-// Each warp first sorts a run of 32*E keys in registers with a bitonic
-// network (shuffles across lanes), then merge-path passes double the run
-// width.  Keys live at padded indices so that lanes reading runs of
-// consecutive keys hit distinct banks.
+// block_radix_sort: stable LSD radix sort of (key, value) pairs of a block,
+// 4-bit digits.  Every thread holds ITEMS consecutive pairs in registers and
+// counts its digits in private 16-bit counters in shared memory (two digits
+// per word); one raking scan over all counters (digit-major, thread-minor)
+// gives every pair its place, and the pairs are scattered to a padded
+// scratch buffer and reloaded for the next digit.  No atomics, no warp votes:
+// about twenty-five instructions per pair and digit, four block barriers.
+//
+// block_unique_sum: merges runs of equal keys of a sorted buffer into
+// (key, sum of the values) pairs, in order.
 #pragma once
 
 #include <cuda_runtime.h>
+
+#include "cm_device.cuh"
 
 namespace cm {
 
@@ -22,107 +30,184 @@ __host__ __device__ constexpr int padded_k(int n) {
   return sizeof(K) == 4 ? n + (n >> 5) + 1 : n + (n >> 4) + 1;
 }
 
-// Bitonic sort of the 32*E keys a warp holds, E per lane in blocked order
-// (lane l holds elements l*E .. l*E+E-1), ascending.  Exchanges across lanes
-// use shuffles; no shared memory, no barriers.
-template <typename K, int E>
-__device__ __forceinline__ void warp_bitonic_sort(K (&v)[E]) {
-  const int lane = threadIdx.x & 31;
+// A (key, value) pair: 8 bytes for 32-bit keys, 16 for 64-bit keys.
+template <typename K> struct SortPair;
+template <> struct __align__(8) SortPair<unsigned> {
+  unsigned k;
+  int v;
+};
+template <> struct __align__(16) SortPair<unsigned long long> {
+  unsigned long long k;
+  int v;
+  int pad;
+};
+template <typename K>
+__device__ __forceinline__ SortPair<K> make_pair_kv(K k, int v) {
+  SortPair<K> p;
+  p.k = k;
+  p.v = v;
+  return p;
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Slot of pair i in a padded scratch buffer: one spare slot after every 8
+// pairs, so that a thread reading its 8 (or 16) consecutive pairs does not
+// share banks with its neighbours.
+__host__ __device__ __forceinline__ int rslot(int i) { return i + (i >> 3); }
+__host__ __device__ constexpr int rslots(int cap) { return cap + cap / 8 + 1; }
+
+constexpr int kDigitBits = 4;
+// Shared scratch of the sort and the unique pass for NT threads.
+template <int NT>
+struct SortScratch {
+  // counter words: word (p, t) at p * (NT + NT/32) + t + t/32 holds thread
+  // t's counts of digits p (low half) and p + 8 (high half)
+  unsigned ctr[8 * (NT + NT / 32) + 1];
+  unsigned wsum[NT / 32];
+  int tab[NT];  // per (round, warp) head counts of the unique pass
+  int scan[NT / 32 + 1];
+};
+
+// Stable ascending sort of the n pairs held at work[rslot(i)], i < n, by the
+// low `bits` bits of their keys (the keys' other bits must be zero).  The
+// result is left at work[0..n) in plain layout.  n <= NT * ITEMS.  All NT
+// threads call it; it ends with a block barrier.
+template <typename K, int NT, int ITEMS>
+__device__ __forceinline__ void block_radix_sort(SortPair<K> *work, SortScratch<NT> &S, int n, int bits) {
+  constexpr int NW = NT / 32, kStride = NT + NT / 32;
+  static_assert(ITEMS >= 1 && ITEMS <= 16 && NT % 32 == 0 && NT * ITEMS <= 65535, "block_radix_sort shape");
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  // every thread holds kmax consecutive pairs (pairs past n sort last); the
+  // other register slots stay idle, so the work follows n, not the capacity
+  const int kmax = (n + NT - 1) / NT;
+  unsigned *const cmine = S.ctr + t + (t >> 5);  // word (0, t)
+  const int rt = (8 * t) % NT;                    // raking: words (8t / NT, rt .. rt + 7)
+  unsigned *const crake = S.ctr + ((8 * t) / NT) * kStride + rt + (rt >> 5);
+  SortPair<K> it[ITEMS];
 #pragma unroll
-  for (int size = 2; size <= 32 * E; size <<= 1) {
+  for (int k = 0; k < ITEMS; ++k) {
+    const int i = t * kmax + k;
+    it[k] = (k < kmax && i < n) ? work[rslot(i)] : make_pair_kv<K>(~(K)0, 0);
+  }
+  const int passes = bits > 0 ? (bits + kDigitBits - 1) / kDigitBits : 1;
+  for (int pass = 0; pass < passes; ++pass) {
+    const int shift = pass * kDigitBits;
+    const bool last = pass == passes - 1;
 #pragma unroll
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      if (stride >= E) {
-        const int ls = stride / E;
-        const bool lower = (lane & ls) == 0;
+    for (int p = 0; p < 8; ++p) cmine[p * kStride] = 0u;
+    unsigned lr[ITEMS];
 #pragma unroll
-        for (int j = 0; j < E; ++j) {
-          const bool asc = ((lane * E + j) & size) == 0;
-          const K o = __shfl_xor_sync(0xffffffffu, v[j], ls);
-          v[j] = (lower == asc) ? min(v[j], o) : max(v[j], o);
-        }
-      } else {
+    for (int k = 0; k < ITEMS; ++k) {
+      lr[k] = 0u;
+      if (k < kmax) {
+        const unsigned d = (unsigned)(it[k].k >> shift) & 15u;
+        unsigned *const w = cmine + (d & 7u) * kStride;
+        const unsigned h = (d & 8u) << 1;
+        const unsigned c = *w;
+        lr[k] = (c >> h) & 0xffffu;
+        *w = c + (1u << h);
+      }
+    }
+    __syncthreads();
+    unsigned cw[8], sum = 0u;
 #pragma unroll
-        for (int j = 0; j < E; ++j) {
-          const int l = j ^ stride;
-          if (l > j) {
-            const bool asc = ((lane * E + j) & size) == 0;
-            const K lo = min(v[j], v[l]), hi = max(v[j], v[l]);
-            v[j] = asc ? lo : hi;
-            v[l] = asc ? hi : lo;
-          }
+    for (int j = 0; j < 8; ++j) {
+      const unsigned x = crake[j];
+      cw[j] = sum;
+      sum += x;  // both halves at once; no half reaches 2^16
+    }
+    unsigned inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    unsigned base = inc - sum, total;
+    if (NW == 1) {
+      total = __shfl_sync(0xffffffffu, inc, 31);
+    } else {
+      if (lane == 31) S.wsum[warp] = inc;
+      __syncthreads();
+      const unsigned v = lane < NW ? S.wsum[lane] : 0u;
+      unsigned vi = v;
+#pragma unroll
+      for (int o = 1; o < NW; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, vi, o);
+        if (lane >= o) vi += y;
+      }
+      base += __shfl_sync(0xffffffffu, vi - v, warp);
+      total = __shfl_sync(0xffffffffu, vi, NW - 1);
+    }
+    base += (total & 0xffffu) << 16;  // digits 8..15 follow every digit 0..7
+#pragma unroll
+    for (int j = 0; j < 8; ++j) crake[j] = base + cw[j];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+      if (k < kmax) {
+        const unsigned d = (unsigned)(it[k].k >> shift) & 15u;
+        const unsigned c = cmine[(d & 7u) * kStride];
+        const int pos = (int)(((c >> ((d & 8u) << 1)) & 0xffffu) + lr[k]);
+        if (last) {
+          if (pos < n) work[pos] = it[k];
+        } else {
+          work[rslot(pos)] = it[k];
         }
       }
+    }
+    __syncthreads();
+    if (!last) {
+#pragma unroll
+      for (int k = 0; k < ITEMS; ++k)
+        if (k < kmax) it[k] = work[rslot(t * kmax + k)];
     }
   }
 }
 
-// Sort of keys only (ascending), stored at padk<K>(i).  Runs of 32*E keys are
-// sorted by one warp each in registers; merge-path passes then double the run
-// width up to n.  The tail up to a multiple of 32*E is filled with all-ones
-// keys, which must not occur in the data; a and b hold padded_k<K>(n rounded
-// up to 32*E) keys.  Returns 0 if the result is in a, 1 if in b.  All NT
-// threads must call it.
-template <typename K, int NT, int E>
-__device__ int block_sort_keys(K *a, K *b, int n) {
-  constexpr int W = 32 * E;
-  const K kMax = ~(K)0;
-  const int npad = ((n + W - 1) / W) * W;
+// Visits the runs of equal keys of the sorted pairs s[0..n): for each run,
+// emit(key, sum of the run's values (wrapping like int atomicAdd), q) with q
+// the run's index in key order.  Returns the number of runs.  n <= NT * 32.
+// All NT threads call it; it ends with a block barrier.
+template <typename K, int NT, int ITEMS, typename F>
+__device__ __forceinline__ int block_unique_emit(const SortPair<K> *s, int n, SortScratch<NT> &S, F emit) {
+  constexpr int NW = NT / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int q = warp; q * W < npad; q += NT / 32) {
-    K v[E];
+  const int rounds = (n + NT - 1) / NT;  // <= ITEMS
+  const unsigned below = lanemask_lt();
+  unsigned hm[ITEMS];
 #pragma unroll
-    for (int j = 0; j < E; ++j) {
-      const int i = q * W + lane * E + j;
-      v[j] = i < n ? a[padk<K>(i)] : kMax;
+  for (int r = 0; r < ITEMS; ++r) {
+    hm[r] = 0u;
+    if (r < rounds) {
+      const int i = r * NT + threadIdx.x;
+      const bool head = i < n && (i == 0 || s[i].k != s[i - 1].k);
+      hm[r] = __ballot_sync(0xffffffffu, head);
+      if (lane == 0) S.tab[r * NW + warp] = __popc(hm[r]);
     }
-    warp_bitonic_sort<K, E>(v);
-#pragma unroll
-    for (int j = 0; j < E; ++j) a[padk<K>(q * W + lane * E + j)] = v[j];
   }
   __syncthreads();
-  const int nruns = npad / E;
-  K *src = a, *dst = b;
-  int cur = 0;
-  for (int width = W; width < npad; width <<= 1) {
-    for (int q = threadIdx.x; q < nruns; q += NT) {
-      const int out = q * E;
-      const int ps = (out / (2 * width)) * (2 * width);
-      const int alen = min(width, npad - ps);
-      const int blen = min(width, npad - ps - alen);
-      const int bs = ps + alen;
-      const int diag = out - ps;
-      int i;
-      if (blen == 0) {
-        i = diag;
-      } else if (src[padk<K>(ps + alen - 1)] <= src[padk<K>(bs)]) {
-        i = diag < alen ? diag : alen;
-      } else {
-        int lo = diag > blen ? diag - blen : 0;
-        int hi = diag < alen ? diag : alen;
-        while (lo < hi) {
-          const int mid = (lo + hi) >> 1;
-          if (src[padk<K>(ps + mid)] <= src[padk<K>(bs + diag - 1 - mid)]) lo = mid + 1;
-          else hi = mid;
-        }
-        i = lo;
-      }
-      int j = diag - i;
-      K ka = i < alen ? src[padk<K>(ps + i)] : kMax;
-      K kb = j < blen ? src[padk<K>(bs + j)] : kMax;
+  const int ncell = rounds * NW;  // <= NT
+  int total;
+  const int ex = block_exclusive_scan<NT>(threadIdx.x < ncell ? S.tab[threadIdx.x] : 0, S.scan, &total);
+  if (threadIdx.x < ncell) S.tab[threadIdx.x] = ex;
+  __syncthreads();
 #pragma unroll
-      for (int t = 0; t < E; ++t) {
-        const bool takeA = (j >= blen) || (i < alen && ka <= kb);
-        dst[padk<K>(out + t)] = takeA ? ka : kb;
-        if (takeA) { ++i; ka = i < alen ? src[padk<K>(ps + i)] : kMax; }
-        else { ++j; kb = j < blen ? src[padk<K>(bs + j)] : kMax; }
-      }
+  for (int r = 0; r < ITEMS; ++r) {
+    if (r < rounds && (hm[r] >> lane & 1u)) {
+      const int i = r * NT + threadIdx.x;
+      const K key = s[i].k;
+      unsigned sum = (unsigned)s[i].v;
+      for (int j = i + 1; j < n && s[j].k == key; ++j) sum += (unsigned)s[j].v;
+      emit(key, (int)sum, S.tab[r * NW + warp] + __popc(hm[r] & below));
     }
-    __syncthreads();
-    K *t = src; src = dst; dst = t;
-    cur ^= 1;
   }
-  return cur;
+  __syncthreads();
+  return total;
 }
 
 }  // namespace cm

@@ -137,8 +137,8 @@ int64_t cm_ctx_launch_count(const cm_ctx *ctx);
  * stages (CM_STAGE_* order); reset != 0 clears the accumulators. */
 enum {
   CM_STAGE_MATCH = 0, /* heavy-edge matching */
-  CM_STAGE_CMAP = 1,  /* coarse-vertex map, row bounds, tile map */
-  CM_STAGE_TILES = 2, /* rows sorted and merged into a stage (tiles; long rows beside them) */
+  CM_STAGE_CMAP = 1,  /* coarse-vertex map, row bounds, row classes */
+  CM_STAGE_ROWS = 2,  /* every coarse row sorted and merged into a stage */
   CM_STAGE_SCAN = 3,  /* cxadj */
   CM_STAGE_COPY = 4,  /* rows from the stage to their final place */
   CM_STAGE_COUNT = 5

@@ -19,10 +19,9 @@ def test_every_parameter_is_a_macro_of_its_source_with_that_default():
 
 
 def test_search_reaches_the_best_valid_point_of_a_separable_cost():
-    # cost: each parameter prefers one candidate; the combination LONG_THR=2048
-    # with CHUNK=4096 is invalid and must never be measured.
+    # cost: each parameter prefers one candidate; the combination TINY_MAX=16
+    # with CHUNK=8192 (nine size classes) is invalid and must never be measured.
     want = {name: cands[-1] for name, _, cands, _ in A.PARAMS}
-    want["CM_CHUNK"] = 8192
     seen = []
 
     def measure(cfg):
@@ -55,8 +54,8 @@ def test_failing_variant_is_skipped():
 
 
 def test_defines_by_source_only_lists_changes():
-    cfg = dict(A.DEFAULTS, CM_LONG_THR=2048, CM_SERIAL_DEG=8)
-    assert A.defines_by_source(cfg) == {"cm_contract.cu": ["-DCM_LONG_THR=2048"],
+    cfg = dict(A.DEFAULTS, CM_TINY_MAX=64, CM_SERIAL_DEG=8)
+    assert A.defines_by_source(cfg) == {"cm_contract.cu": ["-DCM_TINY_MAX=64"],
                                         "cm_match.cu": ["-DCM_SERIAL_DEG=8"]}
     assert A.defines_by_source(dict(A.DEFAULTS)) == {}
 
@@ -64,8 +63,8 @@ def test_defines_by_source_only_lists_changes():
 def test_tuned_defines_from_a_tuning_file(tmp_path):
     p = tmp_path / "tuned.json"
     assert B.tuned_defines(str(p)) == []
-    p.write_text(json.dumps({"defines": {"CM_LONG_THR": 2048, "CM_CHUNK": 8192}, "ms_per_step": 1.0}))
-    assert B.tuned_defines(str(p)) == ["-DCM_CHUNK=8192", "-DCM_LONG_THR=2048"]
+    p.write_text(json.dumps({"defines": {"CM_TINY_MAX": 64, "CM_CHUNK": 8192}, "ms_per_step": 1.0}))
+    assert B.tuned_defines(str(p)) == ["-DCM_CHUNK=8192", "-DCM_TINY_MAX=64"]
     p.write_text(json.dumps({"defines": {"CM_X; rm": 1}}))
     with pytest.raises(ValueError):
         B.tuned_defines(str(p))
