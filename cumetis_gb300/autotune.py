@@ -32,8 +32,10 @@ PARAMS = [
     ("CM_FIRST_KEEP_SHORT", 2, [1, 2, 4], "cm_match.cu"),    # candidates the first round keeps (lane rows)
     ("CM_FIRST_KEEP_CHUNK", 2, [1, 2, 4], "cm_match.cu"),    # ... and per chunked row
     ("CM_TAIL_ITEMS", 4096, [1024, 4096, 16384], "cm_match.cu"),  # rounds this small run in one block
-    ("CM_TINY_MAX", 32, [16, 32, 64], "cm_contract.cu"),    # rows sorted in one-warp batches; larger rows by size class
+    ("CM_TINY_MAX", 64, [16, 32, 64], "cm_contract.cu"),    # rows sorted in one-warp batches; larger rows by size class
     ("CM_CHUNK", 8192, [4096, 8192], "cm_contract.cu"),      # huge-row segment (chunk) size
+    ("CM_CHUNK_THREADS", 1024, [512, 1024], "cm_contract.cu"),  # threads sorting one chunk
+    ("CM_CLASS_ITEMS", 16, [8, 16], "cm_contract.cu"),        # entries per thread of the size-class blocks
     ("CM_MERGE_THREADS", 256, [256, 512], "cm_contract.cu"),
 ]
 DEFAULTS = {name: d for name, d, _, _ in PARAMS}

@@ -43,7 +43,7 @@ __host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v
 // Tiny units: rows of at most kTinyMax entries, D = kTinyDiag diagonals per
 // unit, one warp per unit (capacity 2D entries, at most D/2 non-empty rows).
 #ifndef CM_TINY_MAX
-#define CM_TINY_MAX 32
+#define CM_TINY_MAX 64
 #endif
 constexpr int kTinyMax = CM_TINY_MAX;
 constexpr int kTinyDiag = 2 * kTinyMax;
@@ -57,16 +57,30 @@ static_assert(kTinyMax == 16 || kTinyMax == 32 || kTinyMax == 64, "CM_TINY_MAX: 
 #ifndef CM_CHUNK
 #define CM_CHUNK 8192
 #endif
+#ifndef CM_CHUNK_THREADS
+#define CM_CHUNK_THREADS 1024
+#endif
 constexpr int kChunk = CM_CHUNK;
-constexpr int kChunkThreads = 512;
+constexpr int kChunkThreads = CM_CHUNK_THREADS;
 constexpr int kChunkItems = kChunk / kChunkThreads;
 static_assert(kChunk == 4096 || kChunk == 8192, "CM_CHUNK: 4096 or 8192");
+static_assert(kChunkItems >= 1 && kChunkItems <= 16 && kChunkItems * kChunkThreads == kChunk, "CM_CHUNK_THREADS");
 // Row classes k = 0 .. : kTinyMax * 2^k < L <= kTinyMax * 2^(k+1), up to
-// kChunk; the block of class k has max(32, cap / 16) threads.
+// kChunk; the block of class k has max(32, cap / kClassItems) threads.
+#ifndef CM_CLASS_ITEMS
+#define CM_CLASS_ITEMS 16
+#endif
+constexpr int kClassItems = CM_CLASS_ITEMS;
+static_assert(kClassItems == 4 || kClassItems == 8 || kClassItems == 16, "CM_CLASS_ITEMS: 4, 8 or 16");
 constexpr int kClasses = ilog2(kChunk / kTinyMax);
 static_assert(kClasses <= kRowClasses, "row classes");
 constexpr int class_cap_entries(int k) { return kTinyMax << (k + 1); }
-constexpr int class_threads(int k) { return class_cap_entries(k) / 16 < 32 ? 32 : class_cap_entries(k) / 16; }
+constexpr int class_threads(int k) {
+  return class_cap_entries(k) / kClassItems < 32 ? 32 : class_cap_entries(k) / kClassItems;
+}
+// Rows above kCopySplit expanded entries are copied one block per row, the
+// others 32 rows per warp.
+constexpr int kCopySplit = 256;
 constexpr int class_items(int k) { return class_cap_entries(k) / class_threads(k); }
 constexpr int kCopyBatch = 4;  // stage loads in flight per thread before their stores
 
@@ -427,10 +441,10 @@ k_tiny_units(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, con
       qbase += __popc(hm[r]);
     }
     __syncwarp();
-    if (lane < nnz) {
-      const int c = clo + (int)S.nz_row[lane];
-      S.rdst[lane] = eoff[c];
-      ucount[c] = S.rcount[lane];
+    for (int j = lane; j < nnz; j += 32) {
+      const int c = clo + (int)S.nz_row[j];
+      S.rdst[j] = eoff[c];
+      ucount[c] = S.rcount[j];
     }
     __syncwarp();
     qbase = 0;
@@ -496,9 +510,12 @@ k_count_scan(const int *__restrict__ ucount, const int *d_cn, int *__restrict__ 
   }
 }
 
-// Moves every row of at most kChunk expanded entries from the stage
-// (stage[eoff[c] ..], ucount[c] entries) to its final place cxadj[c]: one warp
-// per row, kCopyBatch loads in flight per lane.
+// Moves every row of at most kCopySplit expanded entries from the stage
+// (stage[eoff[c] ..], ucount[c] entries) to its final place cxadj[c].  A warp
+// takes 32 consecutive rows: lane l loads row l's offsets and count, a warp
+// scan lays the rows' entries out back to back, and the warp then walks them
+// 32 at a time (kCopyBatch steps in flight), each lane finding its entry's
+// row by a five-step search over the prefixes held in the lanes.
 constexpr int kCopyThreads = 256;
 __global__ void __launch_bounds__(kCopyThreads)
 k_copy_rows(const int *d_cn, const int *__restrict__ eoff, const int *__restrict__ ucount,
@@ -507,26 +524,44 @@ k_copy_rows(const int *d_cn, const int *__restrict__ eoff, const int *__restrict
   const int lane = threadIdx.x & 31;
   const int nc = *d_cn;
   const long long warps = (long long)gridDim.x * (kCopyThreads / 32);
-  for (long long c = (long long)blockIdx.x * (kCopyThreads / 32) + (threadIdx.x >> 5); c < nc; c += warps) {
-    const int e0 = eoff[c];
-    if (eoff[c + 1] - e0 > kChunk) continue;  // chunked: its own copy
-    const int cnt = ucount[c];
-    const int dst = cxadj[c];
-    for (int k0 = lane; k0 < cnt; k0 += 32 * kCopyBatch) {
+  for (long long base = ((long long)blockIdx.x * (kCopyThreads / 32) + (threadIdx.x >> 5)) * 32; base < nc;
+       base += warps * 32) {
+    const long long c = base + lane;
+    int src = 0, cnt = 0, dst = 0;
+    if (c < nc) {
+      const int e0 = eoff[c];
+      if (eoff[c + 1] - e0 <= kCopySplit) {  // longer rows: one block each
+        src = e0;
+        cnt = ucount[c];
+        dst = cxadj[c];
+      }
+    }
+    const int incl = warp_inclusive_scan_i32(cnt);
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int excl = incl - cnt;
+    for (int k0 = 0; k0 < total; k0 += 32 * kCopyBatch) {
       int2 e[kCopyBatch];
+      int d[kCopyBatch];
 #pragma unroll
       for (int q = 0; q < kCopyBatch; ++q) {
-        const int k = k0 + 32 * q;
-        e[q] = k < cnt ? __ldcs(stage + e0 + k) : make_int2(0, 0);
-      }
+        const int k = k0 + 32 * q + lane;
+        int r = 0;  // the last row whose first entry is at or before k
 #pragma unroll
-      for (int q = 0; q < kCopyBatch; ++q) {
-        const int k = k0 + 32 * q;
-        if (k < cnt) {
-          cadjncy[dst + k] = e[q].x;
-          cadjwgt[dst + k] = e[q].y;
+        for (int step = 16; step > 0; step >>= 1) {
+          const int v = __shfl_sync(0xffffffffu, excl, r + step);
+          if (v <= k) r += step;
         }
+        const int off = k - __shfl_sync(0xffffffffu, excl, r);
+        const int s0 = __shfl_sync(0xffffffffu, src, r), d0 = __shfl_sync(0xffffffffu, dst, r);
+        d[q] = k < total ? d0 + off : -1;
+        e[q] = k < total ? __ldcs(stage + s0 + off) : make_int2(0, 0);
       }
+#pragma unroll
+      for (int q = 0; q < kCopyBatch; ++q)
+        if (d[q] >= 0) {
+          cadjncy[d[q]] = e[q].x;
+          cadjwgt[d[q]] = e[q].y;
+        }
     }
   }
 }
@@ -751,6 +786,46 @@ k_long_dedup(const int *__restrict__ long_list, const int *__restrict__ chunk_ro
     if (threadIdx.x == 0) {
       chunk_cnt[q] = carry;
       atomicAdd(&ucount[c], carry);
+    }
+  }
+}
+
+// Moves the class rows above kCopySplit expanded entries from the stage to
+// their final place: one block per row, kCopyBatch loads in flight per
+// thread.
+__global__ void __launch_bounds__(256)
+k_copy_class_rows(const int *__restrict__ class_list, const int *__restrict__ class_ctr, long long m,
+                  const int *__restrict__ eoff, const int *__restrict__ ucount, const int *__restrict__ cxadj,
+                  const int2 *__restrict__ stage, int *__restrict__ cadjncy, int *__restrict__ cadjwgt) {
+  constexpr int k0 = ilog2(kCopySplit / kTinyMax);  // first class copied here
+  int cnt[kClasses], total = 0;
+#pragma unroll
+  for (int k = 0; k < kClasses; ++k) {
+    cnt[k] = k >= k0 ? class_ctr[k] : 0;
+    total += cnt[k];
+  }
+  for (int i = blockIdx.x; i < total; i += gridDim.x) {
+    int k = 0, j = i;
+    while (j >= cnt[k]) j -= cnt[k++];
+    const int c = class_list[class_offset(m, kTinyMax, k) + j];
+    const int n = ucount[c];
+    const int2 *src = stage + eoff[c];
+    const long long dst = cxadj[c];
+    for (int t0 = threadIdx.x; t0 < n; t0 += kCopyBatch * 256) {
+      int2 e[kCopyBatch];
+#pragma unroll
+      for (int u = 0; u < kCopyBatch; ++u) {
+        const int t = t0 + u * 256;
+        e[u] = t < n ? __ldcs(src + t) : make_int2(0, 0);
+      }
+#pragma unroll
+      for (int u = 0; u < kCopyBatch; ++u) {
+        const int t = t0 + u * 256;
+        if (t < n) {
+          cadjncy[dst + t] = e[u].x;
+          cadjwgt[dst + t] = e[u].y;
+        }
+      }
     }
   }
 }
@@ -987,18 +1062,24 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
 
   // Every row's unique entries to their final place.
   stage_begin(ctx, s);
-  if (chunked) {
+  const bool big_copy = row_bound > kCopySplit;
+  if (big_copy) {
     cudaEventRecord(ctx->fork_ev, s);
     cudaStreamWaitEvent(ctx->aux[0], ctx->fork_ev, 0);
-    k_long_copy<<<grid_for(sms * 4, m / kChunk + 1), 256, 0, ctx->aux[0]>>>(
-        long_list, chunk_row, eoff, ctr, stage0, stage1, chunk_cnt, coarse->xadj, coarse->adjncy, coarse->adjwgt);
+    k_copy_class_rows<<<grid_for(sms * 8, m / kCopySplit + 1), 256, 0, ctx->aux[0]>>>(
+        class_list, class_ctr, (long long)m, eoff, ucount, coarse->xadj, stage1, coarse->adjncy, coarse->adjwgt);
     ctx->launches++;
+    if (chunked) {
+      k_long_copy<<<grid_for(sms * 4, m / kChunk + 1), 256, 0, ctx->aux[0]>>>(
+          long_list, chunk_row, eoff, ctr, stage0, stage1, chunk_cnt, coarse->xadj, coarse->adjncy, coarse->adjwgt);
+      ctx->launches++;
+    }
     cudaEventRecord(ctx->join_ev[0], ctx->aux[0]);
   }
-  k_copy_rows<<<grid_for((int64_t)sms * 8, n / (kCopyThreads / 32) + 1), kCopyThreads, 0, s>>>(
+  k_copy_rows<<<grid_for((int64_t)sms * 8, n / kCopyThreads + 1), kCopyThreads, 0, s>>>(
       d_sizes, eoff, ucount, coarse->xadj, stage1, coarse->adjncy, coarse->adjwgt);
   ctx->launches++;
-  if (chunked) cudaStreamWaitEvent(s, ctx->join_ev[0], 0);
+  if (big_copy) cudaStreamWaitEvent(s, ctx->join_ev[0], 0);
   stage_end(ctx, CM_STAGE_COPY, s);
   return check_launch(ctx, "contract");
 }
