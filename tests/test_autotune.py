@@ -54,8 +54,8 @@ def test_failing_variant_is_skipped():
 
 
 def test_defines_by_source_only_lists_changes():
-    cfg = dict(A.DEFAULTS, CM_TINY_MAX=64, CM_SERIAL_DEG=8)
-    assert A.defines_by_source(cfg) == {"cm_contract.cu": ["-DCM_TINY_MAX=64"],
+    cfg = dict(A.DEFAULTS, CM_TINY_MAX=32, CM_SERIAL_DEG=8)
+    assert A.defines_by_source(cfg) == {"cm_contract.cu": ["-DCM_TINY_MAX=32"],
                                         "cm_match.cu": ["-DCM_SERIAL_DEG=8"]}
     assert A.defines_by_source(dict(A.DEFAULTS)) == {}
 
