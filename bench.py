@@ -40,6 +40,23 @@ WORKLOADS = {
     "grid725": (lambda cm: cm.gen_grid2d(725, 725), 64, "2D 5-point grid 725x725, unit weights, k=64"),
     "tri69": (lambda cm: cm.gen_tri_grid(69, 69), 8, "2D triangulated grid 69x69, unit weights, k=8"),
 }
+# The same workloads built by the oracle's restated generators (identical
+# graphs, tests/test_oracle.py), so that the CPU reference arm never loads the
+# product library.
+REF_WORKLOADS = {
+    "rmat22": lambda O: O.gen_rmat(22, 16, 0.57, 0.19, 0.19, 1, 1, 100),
+    "rmat20": lambda O: O.gen_rmat(20, 16, 0.57, 0.19, 0.19, 1, 1, 100),
+    "grid725": lambda O: O.gen_grid2d(725, 725),
+    "tri69": lambda O: O.gen_tri_grid(69, 69),
+}
+
+
+def coarsen_threshold(nvtxs, nparts):
+    """k-way Coarsen_threshold = max(n / (20 log2 k), 30 k), cuMetis.cu:3634."""
+    lg, k = 0, nparts
+    while k > 1:
+        lg, k = lg + 1, k >> 1
+    return max(nvtxs // (20 * lg) if lg > 0 else nvtxs, 30 * nparts)
 
 
 def measured_peaks():
@@ -145,13 +162,11 @@ def run_reference(args, ws, rank):
     """CPU baseline arm: the reference's CPU coarsening (restated) on the host."""
     if rank != 0:
         return
-    import cumetis_gb300 as cm
     from oracle import oracle as O
-    gen, k, desc = WORKLOADS[args.workload]
-    g = gen(cm)
-    og = O.CSR(g.xadj, g.adjncy, g.adjwgt, g.vwgt)
-    thr = args.coarsen_to or cm.coarsen_threshold(g.nvtxs, k)
-    mv = O.maxvwgt_rule(int(g.vwgt.sum()), thr)
+    _, k, desc = WORKLOADS[args.workload]
+    og = REF_WORKLOADS[args.workload](O)
+    thr = args.coarsen_to or coarsen_threshold(og.n, k)
+    mv = O.maxvwgt_rule(int(og.vwgt.sum()), thr)
 
     def step():
         O.srand(1)
@@ -181,7 +196,7 @@ def run_reference(args, ws, rank):
     line = {"metric": "coarsened edges/s", "value": v, "unit": "edges/s", "n_gpus": args.gpus, "steps": done,
             "warmup": 1, "ms_per_step": dt * 1e3 / done, "steps_requested": args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": args.workload, "description": desc, "nvtxs": g.nvtxs, "nedges": g.nedges,
+            "config": {"workload": args.workload, "description": desc, "nvtxs": og.n, "nedges": og.m,
                        "nparts": k, "coarsen_threshold": thr, "maxvwgt": mv},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "edges/s", "cores": 1, "kind": "port",
@@ -385,6 +400,8 @@ def main():
     ap.add_argument("--coarsen-to", type=int, default=0,
                     help="coarsening threshold in place of the reference's rule max(n/(20 log2 k), 30k)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode0-steps", type=int, default=5,
+                    help="steps timed with lowest-id ties (the contract's rule) beside a --mode 1 run")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffers) measurement")
     ap.add_argument("--e2e-pipes", type=int, default=4, help="host threads (contexts) taking alternate e2e steps")
     args = ap.parse_args()
@@ -444,11 +461,12 @@ def main():
     ms = allreduce_max(ms, ws, dev)
     value = units_per_step * ws / (ms / 1e3)
 
-    # ---- roofline of the dominant kernel -----------------------------------
-    # The matching (k_match_prep, k_match_first and the persistent round kernel
-    # k_match, back to back on one stream, bracketed by CUDA events) is the
-    # largest single-stream stage.  The contraction stages run several
-    # kernels on several streams; they are reported as one group beside it.
+    # ---- roofline of the dominant stage ------------------------------------
+    # The contraction (k_cmap, the row sorts of every size class on several
+    # streams, the count scan and the copy; CUDA events on the caller's
+    # stream bracket each stage) is the larger part of the step; the matching
+    # (k_match_prep, k_match_first, the round kernel k_match, k_match_finish)
+    # is reported beside it in config.stage_roofline.
     peak, peak_kind = measured_peaks()
     lb = level_bytes(sizes)
     n0, m0 = sizes[0]
@@ -470,19 +488,38 @@ def main():
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            traffic = json.load(f).get(args.workload, {}).get("k_match")
+            traffic = json.load(f).get(args.workload, {}).get("contraction")
     except Exception:
         pass
+    dom = max(group_ms, key=lambda k_: group_ms[k_])
     roof = None
     nlev = max(len(pairs), 1)
-    if group_ms["k_match"] > 0:
-        per_launch_bytes = group_bytes["k_match"] / nlev
-        per_launch_ms = group_ms["k_match"] / nlev
+    if group_ms[dom] > 0:
+        per_launch_bytes = group_bytes[dom] / nlev
+        per_launch_ms = group_ms[dom] / nlev
         ach = per_launch_bytes / (per_launch_ms / 1e3) / 1e9
-        roof = {"kernel": "k_match (with k_match_prep, k_match_first, k_match_finish)", "bound": "hbm", "achieved": ach, "peak": peak,
-                "unit": "GB/s",
-                "frac": ach / peak, "peak_kind": peak_kind, "traffic": traffic,
+        label = {"contraction": "contraction (k_cmap, k_tiny_units, k_class_rows, k_long_sort/merge/dedup, "
+                                "k_count_scan, k_copy_rows, k_copy_class_rows, k_long_copy)",
+                 "k_match": "k_match (with k_match_prep, k_match_first, k_match_finish)"}[dom]
+        roof = {"kernel": label, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak, "peak_kind": peak_kind, "traffic": traffic if dom == "contraction" else None,
                 "bytes_per_launch": per_launch_bytes, "ms_per_launch": per_launch_ms}
+
+    # ---- the contract's own tie rule (lowest vertex id) --------------------
+    mode0_ms = None
+    if args.mode != 0 and args.mode0_steps > 0:
+        def step0():
+            h = ctx.coarsen(dg, thr, 0)
+            h.close()
+        step0()
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.mode0_steps):
+            step0()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        mode0_ms = f0.elapsed_time(f1) / args.mode0_steps
     level_ach = sum(lb) / (ms / 1e3) / 1e9
 
     # ---- end to end through the C ABI with pinned host buffers --------------
@@ -542,8 +579,18 @@ def main():
         e2e_ms = allreduce_max(e2e_ms, ws, dev)
         for c in ctxs[1:]:
             c.close()
+        # one request alone, no overlap: the latency a single caller sees
+        lat = []
+        for _ in range(max(1, min(5, args.steps))):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            e2e_step(0)
+            torch.cuda.synchronize()
+            lat.append((time.perf_counter() - t1) * 1e3)
         e2e = {"value": units_per_step * ws / (e2e_ms / 1e3), "unit": "edges/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "steps": e2e_steps, "pipelines": pipes}
+               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "steps": e2e_steps, "pipelines": pipes,
+               "kind": "throughput of %d pipelined contexts whose steps overlap (not a per-request latency)" % pipes,
+               "single_request_ms": float(np.median(lat))}
 
     line = {"metric": "coarsened edges/s", "value": value, "unit": "edges/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -553,6 +600,7 @@ def main():
                        "parallelism": "replicas" if ws > 1 else "single-gpu",
                        "l2": "inputs larger than L2 (%.0f MB of CSR)" % (4 * (2 * n0 + 2 * m0) / 1e6),
                        "level_roofline_frac": level_ach / peak, "level_achieved_gbs": level_ach,
+                       "mode0_ms_per_step": mode0_ms,
                        "stage_ms_per_step": per_step_ms, "stage_roofline": stage_roofline},
             "roofline": roof, "clocks": clk, "gpu_launches": launches, "e2e": e2e}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

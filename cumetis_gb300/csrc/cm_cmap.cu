@@ -187,16 +187,24 @@ constexpr int kNoAllocWords = kNoAllocStatusWords + kNoAllocTiles + 2;  // 65,58
 static __device__ __align__(256) unsigned long long g_cmap_noalloc_scratch[kNoAllocWords];
 
 // In host code the array's name is only a stand-in; the device address comes
-// from cudaGetSymbolAddress, looked up once per device with that device
-// current.
+// from cudaGetSymbolAddress, looked up with that device current on the first
+// call that succeeds in doing so (a failed look-up is retried by the next
+// call instead of being remembered).
 constexpr int kNoAllocMaxDevices = 64;
 struct NoAllocDevice {
-  std::once_flag once;
-  cudaError_t err = cudaSuccess;
+  std::mutex mu;
+  bool ready = false;
   unsigned long long *scratch = nullptr;
   int num_sms = 0;
 };
 NoAllocDevice g_noalloc_devices[kNoAllocMaxDevices];
+
+// Reports, in band, what the kernels recorded in the array's status block:
+// *d_cnvtxs becomes -(error code) when an error was recorded.
+__global__ void k_noalloc_report(const DevStatus *st, int *d_cnvtxs) {
+  const int e = st->error;
+  if (e != 0) *d_cnvtxs = -e;
+}
 
 }  // namespace
 }  // namespace cm
@@ -217,11 +225,19 @@ extern "C" int cm_build_cmap_noalloc(int32_t nvtxs, const int32_t *d_xadj, const
   if (e != cudaSuccess) return cuda_status(e, "cm_build_cmap_noalloc: cudaGetDevice");
   if (dev < 0 || dev >= kNoAllocMaxDevices) return cm_fail(CM_ERR_UNSUPPORTED, "cm_build_cmap_noalloc: device %d", dev);
   NoAllocDevice &D = g_noalloc_devices[dev];
-  std::call_once(D.once, [&D, dev]() {
-    D.err = cudaGetSymbolAddress((void **)&D.scratch, g_cmap_noalloc_scratch);
-    if (D.err == cudaSuccess) D.err = cudaDeviceGetAttribute(&D.num_sms, cudaDevAttrMultiProcessorCount, dev);
-  });
-  if (D.err != cudaSuccess || !D.scratch) return cuda_status(D.err, "cm_build_cmap_noalloc: scratch set-up");
+  {
+    std::lock_guard<std::mutex> lock(D.mu);
+    if (!D.ready) {
+      unsigned long long *p = nullptr;
+      int sms = 0;
+      e = cudaGetSymbolAddress((void **)&p, g_cmap_noalloc_scratch);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess || !p) return cuda_status(e, "cm_build_cmap_noalloc: scratch set-up");
+      D.scratch = p;
+      D.num_sms = sms;
+      D.ready = true;
+    }
+  }
   cudaStream_t s = (cudaStream_t)stream;
   if (nvtxs == 0) {
     cudaMemsetAsync(d_cnvtxs, 0, sizeof(int32_t), s);
@@ -238,5 +254,6 @@ extern "C" int cm_build_cmap_noalloc(int32_t nvtxs, const int32_t *d_xadj, const
                                           nullptr, INT32_MAX, nullptr, 1, nullptr, nullptr, nullptr, 0, nullptr, lb,
                                           st);
   k_cmap_followers<<<D.num_sms * 8, 256, 0, s>>>(nvtxs, d_match, d_cmap, st);
+  k_noalloc_report<<<1, 1, 0, s>>>(st, d_cnvtxs);
   return cuda_status(cudaGetLastError(), "cm_build_cmap_noalloc launch");
 }

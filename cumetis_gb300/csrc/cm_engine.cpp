@@ -48,6 +48,7 @@ struct Job {
   cm_part_stats stats{};
   Clock::time_point t_submit, t_start, t_end;
   bool done = false;
+  bool waited = false;  // a thread is in cm_engine_wait for this job
 };
 
 // Device bytes a job holds while it runs: the level graphs (input and coarse
@@ -73,6 +74,7 @@ struct cm_engine {
   int64_t inflight = 0;        // footprint of admitted jobs not yet finished
   int64_t next_id = 1;
   bool stop = false;
+  int waiters = 0;             // threads inside cm_engine_wait
   // statistics
   int64_t completed = 0;
   std::vector<double> latencies;
@@ -154,12 +156,30 @@ extern "C" void cm_engine_destroy(cm_engine *e) {
   {
     std::lock_guard<std::mutex> lk(e->mu);
     e->stop = true;
-    // jobs not started are dropped; running ones finish
+    // Jobs not started are dropped: they end with an error, and their
+    // waiters wake up.  Running jobs finish.
+    auto drop = [&](Job *j) {
+      j->status = CM_ERR_INVALID;
+      j->error = "cm_engine_wait: the engine was destroyed before the job ran";
+      j->t_start = j->t_end = Clock::now();
+      j->done = true;
+    };
+    for (Job *j : e->pending) drop(j);
+    for (Job *j : e->ready) {
+      drop(j);
+      e->inflight -= j->footprint;
+    }
     e->pending.clear();
     e->ready.clear();
   }
   e->cv_work.notify_all();
+  e->cv_done.notify_all();
   for (auto &t : e->threads) t.join();
+  {
+    // threads still inside cm_engine_wait leave before the engine goes away
+    std::unique_lock<std::mutex> lk(e->mu);
+    e->cv_done.wait(lk, [&] { return e->waiters == 0; });
+  }
   for (cm_ctx *c : e->ctxs) cm_ctx_destroy(c);
   delete e;
 }
@@ -194,7 +214,11 @@ extern "C" int cm_engine_wait(cm_engine *e, int64_t job_id, int32_t *objval, cm_
   auto it = e->jobs.find(job_id);
   if (it == e->jobs.end()) return cm_fail(CM_ERR_INVALID, "cm_engine_wait: unknown job %lld", (long long)job_id);
   Job *j = it->second.get();
+  if (j->waited) return cm_fail(CM_ERR_INVALID, "cm_engine_wait: job %lld already has a waiter", (long long)job_id);
+  j->waited = true;
+  ++e->waiters;
   e->cv_done.wait(lk, [&] { return j->done; });
+  --e->waiters;
   if (objval) *objval = j->objval;
   if (info) {
     info->queue_ms = ms_between(j->t_submit, j->t_start);
@@ -207,6 +231,7 @@ extern "C" int cm_engine_wait(cm_engine *e, int64_t job_id, int32_t *objval, cm_
   const std::string err = j->error;
   e->jobs.erase(it);
   lk.unlock();
+  e->cv_done.notify_all();  // a destroy may be waiting for the waiters to leave
   if (rc != CM_OK) return cm_fail(rc, "%s", err.c_str());
   return CM_OK;
 }

@@ -195,9 +195,11 @@ int cm_build_cmap(cm_ctx *ctx, int32_t nvtxs, const int32_t *d_xadj, const int32
  * call on a device looks up that array's device address; make that first call
  * before any stream capture.  All calls share the array: calls that overlap
  * on the GPU (other streams, other threads) race and must be serialised by the
- * caller.  Problems the kernels detect (an out-of-range or non-involutive
- * matching, a look-back wait past its time limit) are recorded in the array
- * and not reported; pass only valid matchings, or use cm_build_cmap. */
+ * caller.  Problems the kernels detect are reported in band, once the call's
+ * work has run on the stream: d_cnvtxs[0] then holds -CM_ERR_INVALID (an
+ * out-of-range or non-involutive matching) or -CM_ERR_LIMIT (a look-back wait
+ * past its time limit) instead of n', and the other outputs are not
+ * meaningful.  The next call starts clean. */
 int cm_build_cmap_noalloc(int32_t nvtxs, const int32_t *d_xadj, const int32_t *d_vwgt,
                           const int32_t *d_match, int32_t *d_cmap, int32_t *d_leader,
                           int32_t *d_cvwgt, int32_t *d_eoff, int32_t *d_cnvtxs, void *stream);
@@ -331,13 +333,17 @@ typedef struct cm_job_info {
  * returns CM_ERR_LIMIT when it is full. */
 int  cm_engine_create(int device, int32_t nworkers, int64_t hbm_budget_bytes, int32_t max_queue,
                       int64_t reserve_nvtxs, int64_t reserve_nedges, cm_engine **out);
-/* Lets running jobs finish, drops jobs not started, frees the engine. */
+/* Lets running jobs finish, drops jobs not started (their waiters return
+ * CM_ERR_INVALID), waits until every thread has left cm_engine_wait, and
+ * frees the engine. */
 void cm_engine_destroy(cm_engine *e);
 int  cm_engine_submit(cm_engine *e, const cm_graph *g_host, int32_t nparts, const cm_part_params *params,
                       int32_t *part, int64_t *job_id);
 /* *done = 1 once the job has finished (non-blocking). */
 int  cm_engine_poll(cm_engine *e, int64_t job_id, int32_t *done);
-/* Blocks until the job is done; returns its status (the job is forgotten). */
+/* Blocks until the job is done; returns its status (the job is forgotten).
+ * One waiter per job: a second thread waiting for the same job at the same
+ * time gets CM_ERR_INVALID. */
 int  cm_engine_wait(cm_engine *e, int64_t job_id, int32_t *objval, cm_job_info *info);
 /* Jobs completed and latency percentiles (submit -> end) since the last reset. */
 int  cm_engine_stats(cm_engine *e, int64_t *completed, double *p50_ms, double *p99_ms, int reset);

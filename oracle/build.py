@@ -10,7 +10,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_TREE = os.environ.get("CM_REFERENCE_TREE", "/root/reference")
+# The reference tree: $CM_REFERENCE_TREE, else a directory named "reference"
+# beside this repository.
+REF_TREE = os.environ.get("CM_REFERENCE_TREE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 def _newer(target, sources):

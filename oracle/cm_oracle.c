@@ -23,6 +23,8 @@
  *                      the reference's own CPU coarsening, cu:830-918
  *                      (random-order HEM) and cu:737-825 (hash-table
  *                      contraction), restated; used as the timed CPU baseline
+ *   or_gen_rmat        the R-MAT workload generator of the library, restated
+ *                      (the CPU arm's input, without the product library)
  *
  * Parity pin: tests/golden holds outputs of the reference's CPU coarsening
  * (cuMetis_cpu_match / cuMetis_cpu_create_cgraph, built from the reference
@@ -429,3 +431,89 @@ int64_t or_refine_kway(int32_t n, const int32_t *xadj, const int32_t *adjncy, co
   free(pw); free(acc); free(target); free(flag); free(cnt); free(order);
   return moves;
 }
+
+/* ------------------------------------------------------------------------
+ * or_gen_rmat: the R-MAT workload generator, restated from the library's
+ * cm_gen_rmat (so that the CPU reference arm of the benchmark builds its
+ * input without loading the product library).  Pair e of the edge list draws
+ * one 64-bit splitmix64 hash per two levels from a counter; each 32-bit half
+ * picks a quadrant by the thresholds a, a+b, a+b+c (most significant level
+ * first); self loops and duplicates are dropped, the rest symmetrised, rows
+ * sorted; weights are a hash of the undirected edge in [wmin, wmax].  The
+ * arrays are malloc'd (release with or_free); returns m, or -1.
+ * ---------------------------------------------------------------------- */
+static uint64_t or_mix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+static void or_radix_u64(uint64_t *a, uint64_t *tmp, int64_t n) {
+  size_t *cnt = (size_t *)malloc(sizeof(size_t) << 16);
+  for (int shift = 0; shift < 64; shift += 16) {
+    memset(cnt, 0, sizeof(size_t) << 16);
+    for (int64_t i = 0; i < n; ++i) cnt[(a[i] >> shift) & 0xffff]++;
+    size_t s = 0;
+    for (int d = 0; d < (1 << 16); ++d) { size_t t = cnt[d]; cnt[d] = s; s += t; }
+    for (int64_t i = 0; i < n; ++i) tmp[cnt[(a[i] >> shift) & 0xffff]++] = a[i];
+    uint64_t *x = a; a = tmp; tmp = x;  /* four passes: the result ends in the caller's a */
+    (void)x;
+  }
+  free(cnt);
+}
+
+int64_t or_gen_rmat(int32_t scale, int32_t edge_factor, double a, double b, double c, uint64_t seed, int32_t wmin,
+                    int32_t wmax, int32_t **xadj_out, int32_t **adjncy_out, int32_t **adjwgt_out) {
+  if (scale < 1 || scale > 30 || edge_factor < 1 || wmin < 1 || wmax < wmin) return -1;
+  const int64_t n = (int64_t)1 << scale, ne = (int64_t)edge_factor << scale;
+  const uint64_t ta = (uint64_t)(a * 4294967296.0), tb = (uint64_t)((a + b) * 4294967296.0),
+                 tc = (uint64_t)((a + b + c) * 4294967296.0);
+  const uint64_t s0 = or_mix64(seed ^ 0x52414D4147454E31ull);
+  uint64_t *keys = (uint64_t *)malloc(sizeof(uint64_t) * ne), *tmp = (uint64_t *)malloc(sizeof(uint64_t) * ne);
+  if (!keys || !tmp) { free(keys); free(tmp); return -1; }
+  for (int64_t e = 0; e < ne; ++e) {
+    uint64_t u = 0, v = 0;
+    for (int l = 0; l < scale; l += 2) {
+      const uint64_t r = or_mix64(s0 + (uint64_t)e * 32 + (uint64_t)(l >> 1));
+      for (int h = 0; h < 2 && l + h < scale; ++h) {
+        const uint64_t x = h ? (r >> 32) : (r & 0xffffffffu);
+        const uint64_t bu = x >= tb, bv = (x >= ta && x < tb) || x >= tc;
+        u = (u << 1) | bu;
+        v = (v << 1) | bv;
+      }
+    }
+    const uint64_t lo = u < v ? u : v, hi = u < v ? v : u;
+    keys[e] = lo == hi ? ~0ull : ((lo << 32) | hi);
+  }
+  or_radix_u64(keys, tmp, ne);
+  free(tmp);
+  int64_t w = 0;
+  for (int64_t i = 0; i < ne && keys[i] != ~0ull; ++i)
+    if (w == 0 || keys[i] != keys[w - 1]) keys[w++] = keys[i];
+  const int64_t m = 2 * w;
+  int32_t *xadj = (int32_t *)calloc(n + 1, sizeof(int32_t));
+  int32_t *adjncy = (int32_t *)malloc(sizeof(int32_t) * (m > 0 ? m : 1));
+  int32_t *adjwgt = (int32_t *)malloc(sizeof(int32_t) * (m > 0 ? m : 1));
+  int32_t *pos = (int32_t *)malloc(sizeof(int32_t) * n);
+  if (!xadj || !adjncy || !adjwgt || !pos) { free(keys); free(xadj); free(adjncy); free(adjwgt); free(pos); return -1; }
+  for (int64_t i = 0; i < w; ++i) { xadj[(keys[i] >> 32) + 1]++; xadj[(keys[i] & 0xffffffffu) + 1]++; }
+  for (int64_t i = 0; i < n; ++i) { xadj[i + 1] += xadj[i]; pos[i] = xadj[i]; }
+  const uint64_t wseed = or_mix64(seed ^ 0x5745494748543031ull), span = (uint64_t)(wmax - wmin) + 1;
+  for (int64_t i = 0; i < w; ++i) {
+    const int32_t lo = (int32_t)(keys[i] >> 32), hi = (int32_t)(keys[i] & 0xffffffffu);
+    const int32_t wt = wmin + (int32_t)(or_mix64(wseed ^ keys[i]) % span);
+    int32_t p = pos[lo]++;
+    adjncy[p] = hi; adjwgt[p] = wt;
+    p = pos[hi]++;
+    adjncy[p] = lo; adjwgt[p] = wt;
+  }
+  free(keys);
+  free(pos);
+  *xadj_out = xadj;
+  *adjncy_out = adjncy;
+  *adjwgt_out = adjwgt;
+  return m;
+}
+
+void or_free(void *p) { free(p); }

@@ -311,3 +311,54 @@ def refine_kway_c(g, where, k):
     w = np.array(where, np.int32).copy()
     mv = lib().or_refine_kway(g.n, _p(g.xadj), _p(g.adjncy), _p(g.adjwgt), _p(g.vwgt), int(k), _p(w))
     return w, int(mv)
+
+
+def gen_rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, wmin=1, wmax=100):
+    """The R-MAT workload generator restated in the oracle (or_gen_rmat):
+    the same graph as the library's cm_gen_rmat, without loading it."""
+    L = lib()
+    P = ctypes.POINTER(ctypes.c_int32)
+    L.or_gen_rmat.restype = ctypes.c_int64
+    L.or_gen_rmat.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                              ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(P),
+                              ctypes.POINTER(P), ctypes.POINTER(P)]
+    L.or_free.argtypes = [ctypes.c_void_p]
+    px, pa, pw = P(), P(), P()
+    m = L.or_gen_rmat(int(scale), int(edge_factor), a, b, c, int(seed), int(wmin), int(wmax), ctypes.byref(px),
+                      ctypes.byref(pa), ctypes.byref(pw))
+    if m < 0:
+        raise ValueError("or_gen_rmat: bad parameters")
+    n = 1 << scale
+    xadj = np.ctypeslib.as_array(px, shape=(n + 1,)).copy()
+    adj = np.ctypeslib.as_array(pa, shape=(max(m, 1),))[:m].copy()
+    wt = np.ctypeslib.as_array(pw, shape=(max(m, 1),))[:m].copy()
+    for p in (px, pa, pw):
+        L.or_free(p)
+    return CSR(xadj, adj, wt, np.ones(n, np.int32))
+
+
+def gen_mesh(nx, ny, offsets):
+    """2D mesh with unit weights: vertex (i, j) -> i * ny + j, joined to
+    (i, j) +- each offset; rows sorted (the library's grid generators)."""
+    n = nx * ny
+    ii, jj = np.divmod(np.arange(n, dtype=np.int64), ny)
+    src, dst = [], []
+    for di, dj in offsets:
+        for s in (-1, 1):
+            a, b = ii + s * di, jj + s * dj
+            ok = (a >= 0) & (a < nx) & (b >= 0) & (b < ny)
+            src.append(np.nonzero(ok)[0])
+            dst.append((a * ny + b)[ok])
+    src, dst = np.concatenate(src), np.concatenate(dst)
+    order = np.lexsort((dst, src))
+    xadj = np.zeros(n + 1, np.int64)
+    np.add.at(xadj, src + 1, 1)
+    return CSR(np.cumsum(xadj), dst[order], np.ones(len(dst), np.int32), np.ones(n, np.int32))
+
+
+def gen_grid2d(nx, ny):
+    return gen_mesh(nx, ny, [(0, 1), (1, 0)])
+
+
+def gen_tri_grid(nx, ny):
+    return gen_mesh(nx, ny, [(0, 1), (1, 0), (1, 1)])

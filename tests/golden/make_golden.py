@@ -27,7 +27,7 @@ sys.path.insert(0, ROOT)
 from oracle import oracle as O  # noqa: E402
 import cumetis_gb300 as cm  # noqa: E402
 
-REF_TREE = os.environ.get("CM_REFERENCE_TREE", "/root/reference")
+from oracle.build import REF_TREE  # noqa: E402  ($CM_REFERENCE_TREE, else reference/ beside the repository)
 
 
 def read_mtx_symmetric(path):

@@ -90,3 +90,34 @@ def test_served_result_same_alone_and_in_the_mix(ctx):
     assert abs(c16 - cut_alone16) <= 0.03 * cut_alone16
     pw = np.bincount(p16, weights=target16.vwgt, minlength=16)
     assert pw.max() * 16 / target16.vwgt.sum() < 1.10
+
+
+def test_engine_destroy_wakes_waiters_and_second_waiter_is_refused():
+    """Destroying an engine while a thread waits for a job that has not run
+    yet ends that wait with CM_ERR_INVALID (or the job's result, if it ran
+    first) instead of leaving the thread asleep on freed memory; a second
+    thread waiting for the same job is refused."""
+    import threading
+    import time
+    e = cm.Engine(0, workers=1)
+    big = cm.gen_rmat(16, 16, seed=2)
+    small = cm.gen_grid2d(60, 60)
+    jobs = [e.submit(big, 64)] + [e.submit(small, 4) for _ in range(6)]
+    out = {}
+
+    def waiter(key, job):
+        try:
+            e.wait(job)
+            out[key] = "done"
+        except cm.CMError as ex:
+            out[key] = ex.code
+
+    t1 = threading.Thread(target=waiter, args=("first", jobs[-1]))
+    t1.start()
+    time.sleep(0.05)
+    waiter("second", jobs[-1])  # the first thread is (almost surely) still waiting
+    e.close()
+    t1.join(timeout=120)
+    assert not t1.is_alive()
+    assert out["first"] in ("done", cm.CM_ERR_INVALID)
+    assert out["second"] in ("done", cm.CM_ERR_INVALID)

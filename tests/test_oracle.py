@@ -150,3 +150,15 @@ def test_refine_model_c_equals_python():
         b, mb = O.refine_kway_c(og, where, k)
         np.testing.assert_array_equal(a, b)
         assert ma == mb
+
+
+def test_oracle_generators_equal_the_library_generators():
+    """The CPU arm builds its inputs with the oracle's restated generators;
+    they must produce the library's graphs exactly."""
+    import cumetis_gb300 as cm
+    pairs = [(O.gen_rmat(12, 16, 0.57, 0.19, 0.19, 1, 1, 100), cm.gen_rmat(12, 16, 0.57, 0.19, 0.19, 1, 1, 100)),
+             (O.gen_rmat(9, 8, 0.6, 0.15, 0.15, 7, 1, 5), cm.gen_rmat(9, 8, 0.6, 0.15, 0.15, 7, 1, 5)),
+             (O.gen_grid2d(37, 21), cm.gen_grid2d(37, 21)), (O.gen_tri_grid(19, 23), cm.gen_tri_grid(19, 23))]
+    for og, g in pairs:
+        for f in ("xadj", "adjncy", "adjwgt", "vwgt"):
+            assert np.array_equal(getattr(og, f), getattr(g, f)), f

@@ -161,13 +161,14 @@ def _long_row_graph(L_leader, L_follower, extra=0, seed=0):
     return O.CSR(np.cumsum(xadj), dst, w, np.ones(n))
 
 
-@pytest.mark.parametrize("lens", [(100, 28), (128, 128), (128, 129), (200, 300), (512, 512), (512, 513), (1024, 1024),
-                                  (1024, 1025), (2048, 2048), (2048, 2049), (4096, 4096), (4097, 4096), (20000, 13000),
-                                  (40000, 30000)])
+@pytest.mark.parametrize("lens", [(32, 32), (32, 33), (100, 28), (64, 65), (128, 128), (128, 129), (200, 300),
+                                  (512, 512), (512, 513), (1024, 1024), (1024, 1025), (2048, 2048), (2048, 2049),
+                                  (4096, 4096), (4097, 4096), (20000, 13000), (40000, 30000)])
 def test_long_rows(ctx, lens):
-    """Coarse rows at every path boundary: short rows of a few hundred
-    entries, the tile limit 1024, the size classes 2048 / 4096 / 8192, and far
-    beyond the 8192-entry chunk (chunk sort, merge passes, dedup, copy)."""
+    """Coarse rows at every path boundary: the one-warp batches (up to 64
+    entries), every size class (powers of two up to the 8192-entry chunk), the
+    copy split at 256, and far beyond the chunk (chunk sort, merge passes,
+    dedup, copy)."""
     g = _long_row_graph(*lens, extra=500, seed=sum(lens))
     match = np.arange(g.n, dtype=np.int32)
     match[0], match[1] = 1, 0
@@ -337,11 +338,16 @@ def test_empty_and_tiny(ctx):
 # ---------------------------------------------------------------------------
 # full-size workloads: bit-exact where the oracle finishes in seconds, and
 # size-independent properties otherwise
-def test_grid725_full_size_bitexact(ctx):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_grid725_full_size_bitexact(ctx, mode):
+    """The 725 x 725 grid (k = 64) coarsened to the reference's threshold,
+    every level bit-exact, in both tie orders: lowest id (the rule of the
+    contract) and the edge hash (the partitioner's and the benchmark's
+    default)."""
     g = cm.gen_grid2d(725, 725)
     thr = cm.coarsen_threshold(g.nvtxs, 64)
-    want = O.coarsen(_o(g), thr)
-    h = ctx.coarsen(g, thr)
+    want = O.coarsen(_o(g), thr, mode)
+    h = ctx.coarsen(g, thr, mode)
     assert len(h) == len(want)
     for l, (wg, wm, wc) in enumerate(want):
         hg, hc, hm = h.copy_level(l)
@@ -351,9 +357,9 @@ def test_grid725_full_size_bitexact(ctx):
 
 
 def test_large_ids_use_64bit_tile_keys(ctx):
-    """n above 2^23 - 1 coarse ids: the tiles switch to 64-bit (row, id)
-    keys.  A 2900 x 2900 grid (8,410,000 vertices), both tie orders for the
-    matching, contraction bit-exact against the oracle."""
+    """Many coarse ids: a 2900 x 2900 grid (8,410,000 vertices, ids of 23
+    bits), both tie orders for the matching, contraction bit-exact against
+    the oracle."""
     g = cm.gen_grid2d(2900, 2900)
     assert g.nvtxs > (1 << 23) - 1
     og = _o(g)
