@@ -111,6 +111,7 @@ def _declare(L):
         "cm_contract": (c_int, [c_vp, G, c_vp, c_vp, G, c_vp, c_vp]),
         "cm_coarsen_default_params": (None, [c_i32, c_i32, ctypes.POINTER(cm_coarsen_params)]),
         "cm_coarsen": (c_int, [c_vp, G, c_int, ctypes.POINTER(cm_coarsen_params), ctypes.POINTER(c_vp), c_vp]),
+        "cm_coarsen_batch": (c_int, [c_vp, c_i32, G, ctypes.POINTER(cm_coarsen_params), ctypes.POINTER(c_vp), c_vp]),
         "cm_hierarchy_free": (None, [c_vp]),
         "cm_hierarchy_levels": (c_i32, [c_vp]),
         "cm_hierarchy_level": (c_int, [c_vp, c_i32, G, ctypes.POINTER(c_vp), ctypes.POINTER(c_vp)]),

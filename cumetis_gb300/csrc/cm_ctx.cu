@@ -376,22 +376,6 @@ extern "C" int cm_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *d_m
 // ---------------------------------------------------------------------------
 // multilevel coarsening
 // ---------------------------------------------------------------------------
-struct cm_level {
-  cm_graph g;             // device arrays
-  int32_t *match = nullptr;  // device, n (absent on the coarsest level)
-  int32_t *cmap = nullptr;   // device, n (absent on the coarsest level)
-  void *block = nullptr;     // single allocation backing the arrays
-  bool owns_graph = true;    // false for a caller-owned input on the device
-};
-
-struct cm_hierarchy {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::vector<cm_level> levels;
-  int32_t maxvwgt = 0;
-  std::vector<int32_t> rounds;
-};
-
 extern "C" void cm_coarsen_default_params(int32_t nvtxs, int32_t nparts, cm_coarsen_params *p) {
   if (!p) return;
   // k-way Coarsen_threshold = max(n / (20 log2 k), 30 k), cuMetis.cu:3634
@@ -434,7 +418,7 @@ extern "C" void cm_hierarchy_free(cm_hierarchy *h) {
   for (auto &L : h->levels)
     if (L.block) cudaFreeAsync(L.block, h->stream);
   cudaStreamSynchronize(h->stream);
-  delete h;
+  delete h;  // shared slabs are released with their last hierarchy
 }
 
 extern "C" int cm_coarsen(cm_ctx *ctx, const cm_graph *g, int input_on_device, const cm_coarsen_params *params,

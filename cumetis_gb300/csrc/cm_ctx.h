@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 #include "cm_device.cuh"
@@ -55,6 +56,39 @@ struct cm_ctx {
   int class_blocks_per_sm[8] = {1, 1, 1, 1, 1, 1, 1, 1};
 };
 
+// One coarsening level on the device.
+struct cm_level {
+  cm_graph g{};              // device arrays
+  int32_t *match = nullptr;  // device, n (absent on the coarsest level)
+  int32_t *cmap = nullptr;   // device, n (absent on the coarsest level)
+  void *block = nullptr;     // allocation backing the arrays (freed with the hierarchy), or
+  bool owns_graph = true;    // false for a caller-owned input on the device
+};
+
+// Device memory shared by the levels of several hierarchies (a batch carves
+// every graph's level out of one allocation): freed, stream-ordered, when its
+// last user lets go.
+struct cm_slab {
+  void *ptr = nullptr;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  ~cm_slab() {
+    if (ptr) {
+      cudaSetDevice(device);
+      cudaFreeAsync(ptr, stream);
+    }
+  }
+};
+
+struct cm_hierarchy {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<cm_level> levels;
+  int32_t maxvwgt = 0;
+  std::vector<int32_t> rounds;
+  std::vector<std::shared_ptr<cm_slab>> slabs;  // shared backing of levels carved from a batch
+};
+
 namespace cm {
 
 // Bump-allocates `bytes` (256-byte aligned) from the context workspace for the
@@ -99,8 +133,12 @@ size_t cmap_ws_bytes(int64_t n);
 size_t contract_ws_bytes(int64_t n, int64_t m);
 
 // Stage launchers shared between entry points (no argument checking).
+// vgid/gbase/gcap (optional): several graphs side by side -- vertex v belongs
+// to graph vgid[v], whose first vertex is gbase[g] and whose weight cap is
+// gcap[g]; maxvwgt is then the smallest cap.
 int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, int32_t *d_match,
-                 cudaStream_t s);
+                 cudaStream_t s, const int32_t *vgid = nullptr, const int32_t *gbase = nullptr,
+                 const int32_t *gcap = nullptr);
 // Rows of more than long_threshold expanded entries are listed: up to
 // long_chunk entries by size class (class_offset(m, long_threshold, k) of
 // class_list, counts in class_ctr[k]), longer ones as chunked rows.
@@ -115,3 +153,9 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
                     int32_t *d_sizes, cudaStream_t s, int64_t row_bound);
 
 }  // namespace cm
+
+// Partition of a coarsened graph (cm_refine.cu): the initial partition of the
+// hierarchy's coarsest level on the host, then projection and refinement
+// level by level on the context's stream.  Frees the hierarchy.
+int part_hierarchy(cm_ctx *ctx, cm_hierarchy *h, int32_t nparts, const cm_part_params &P, int32_t *part,
+                   int32_t *objval, cm_part_stats *stats);

@@ -105,6 +105,11 @@ struct MatchArgs {
   DevStatus *st;
   unsigned long long *trace;     // optional: row 0 header, row r+1 = round r
   int trace_rows;
+  // Several independent graphs side by side (a batch): vgid[v] = v's graph,
+  // whose weight cap is gcap[g] and whose first vertex is gbase[g] (the edge
+  // hash of the tie rule is taken on graph-local ids, so a graph matches the
+  // same alone and in a batch).  Null for one graph.
+  const int *vgid, *gbase, *gcap;
 };
 
 // Candidates.  Lex mode (ties to the lower id) packs (weight, ~id) into one
@@ -113,8 +118,9 @@ struct MatchArgs {
 template <bool H> struct Cand;
 template <> struct Cand<false> {
   unsigned long long key = 0ull;
-  __device__ __forceinline__ static Cand make(int v, int k, int w) {
+  __device__ __forceinline__ static Cand make(int v, int k, int w, int hb) {
     (void)v;
+    (void)hb;
     Cand c;
     c.key = ((unsigned long long)((unsigned)w ^ 0x80000000u) << 32) | (unsigned)(~(unsigned)k);
     return c;
@@ -144,11 +150,11 @@ template <> struct Cand<true> {
   int w = 0;
   unsigned h = 0u;
   int k = INT_MAX;  // INT_MAX = none
-  __device__ __forceinline__ static Cand make(int v, int k, int w) {
+  __device__ __forceinline__ static Cand make(int v, int k, int w, int hb) {
     Cand c;
     c.w = w;
     c.k = k;
-    c.h = edge_hash((unsigned)min(v, k), (unsigned)max(v, k));
+    c.h = edge_hash((unsigned)(min(v, k) - hb), (unsigned)(max(v, k) - hb));
     return c;
   }
   __device__ __forceinline__ bool valid() const { return k != INT_MAX; }
@@ -203,22 +209,29 @@ struct TopK {
   }
   // Edge (v, k) of weight w.  In hash mode the edge hash is computed only when
   // the weight can still enter the list (a lighter edge loses to the last
-  // entry whatever its hash); the result is that of insert(make(v, k, w)).
-  __device__ __forceinline__ void insert_edge(int v, int k, int w) {
+  // entry whatever its hash); the result is that of insert(make(v, k, w, hb)).
+  // hb: the first vertex of v's graph (0 for one graph).
+  __device__ __forceinline__ void insert_edge(int v, int k, int w, int hb) {
     if constexpr (H) {
       if (c[KK - 1].valid() && w < c[KK - 1].w) return;
     }
-    insert(Cand<H>::make(v, k, w));
+    insert(Cand<H>::make(v, k, w, hb));
   }
 };
 
+// First vertex of v's graph (the hash base of the tie rule) and its weight cap.
+__device__ __forceinline__ int hash_base(const MatchArgs &a, int v) { return a.vgid ? __ldg(a.gbase + __ldg(a.vgid + v)) : 0; }
+__device__ __forceinline__ long long weight_cap(const MatchArgs &a, int v) {
+  return a.vgid ? (long long)__ldg(a.gcap + __ldg(a.vgid + v)) : a.maxvwgt;
+}
+
 template <bool H>
 __device__ __forceinline__ bool eligible(const MatchArgs &a, long long vw, int v, int k, int s) {
-  (void)v;
   if (k == v || s >= 0) return false;  // self or matched
   const long long vk = -1ll - s;
-  if (vw + vk > a.maxvwgt) return false;
-  return 3 * vw < a.maxvwgt || 3 * vk < a.maxvwgt;
+  const long long cap = weight_cap(a, v);
+  if (vw + vk > cap) return false;
+  return 3 * vw < cap || 3 * vk < cap;
 }
 
 // Merges the lanes' sorted lists into the warp's best KK (all lanes get it).
@@ -256,10 +269,11 @@ __device__ __forceinline__ TopK<H, KK> lane_scan(const MatchArgs &a, int v, long
 #pragma unroll
   for (int u = 0; u < U; ++u) s[u] = (k[u] >= 0 && !all_elig) ? __ldcg(a.m2 + k[u]) : -1;
   TopK<H, KK> t;
+  const int hb = hash_base(a, v);
 #pragma unroll
   for (int u = 0; u < U; ++u)
     if (k[u] >= 0 && (all_elig ? k[u] != v : eligible<H>(a, vw, v, k[u], s[u])))
-      t.insert_edge(v, k[u], w[u]);
+      t.insert_edge(v, k[u], w[u], hb);
   return t;
 }
 
@@ -362,7 +376,7 @@ __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool 
       TopK<H, kFirstKeepShort> tk;
 #pragma unroll
       for (int t = 0; t < kSerialDeg; ++t)
-        if (k[t] >= 0 && k[t] != v) tk.insert_edge(v, k[t], w[t]);
+        if (k[t] >= 0 && k[t] != v) tk.insert_edge(v, k[t], w[t], hash_base(a, v));
       store_top(a, v, tk);
       continue;
     }
@@ -379,14 +393,14 @@ __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool 
 #pragma unroll
       for (int t = 0; t < kSerialDeg; ++t)
         if (k[t] >= 0 && (skip_gather ? k[t] != v : eligible<H>(a, vw, v, k[t], s[t])))
-          tk.insert_edge(v, k[t], a.adjwgt[xs + t]);
+          tk.insert_edge(v, k[t], a.adjwgt[xs + t], hash_base(a, v));
       store_top(a, v, tk);
     } else {
       TopK<H, kTop> tk;
 #pragma unroll
       for (int t = 0; t < kSerialDeg; ++t)
         if (k[t] >= 0 && (skip_gather ? k[t] != v : eligible<H>(a, vw, v, k[t], s[t])))
-          tk.insert_edge(v, k[t], a.adjwgt[xs + t]);
+          tk.insert_edge(v, k[t], a.adjwgt[xs + t], hash_base(a, v));
       store_top(a, v, tk);
     }
   }
@@ -734,7 +748,8 @@ size_t match_ws_bytes(int64_t n, int64_t m) {
   return b + 64 * 256;
 }
 
-int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, int32_t *d_match, cudaStream_t s) {
+int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, int32_t *d_match, cudaStream_t s,
+                 const int32_t *vgid, const int32_t *gbase, const int32_t *gcap) {
   const int n = g->nvtxs;
   if (n == 0) return CM_OK;
   if (mode != CM_MATCH_HEM && mode != CM_MATCH_HEM_HASH)
@@ -743,9 +758,12 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
   MatchArgs a;
   a.n = n;
   a.xadj = g->xadj; a.adjncy = g->adjncy; a.adjwgt = g->adjwgt; a.vwgt = g->vwgt;
-  a.maxvwgt = maxvwgt;
+  a.maxvwgt = maxvwgt;  // with graphs side by side: the smallest cap (it gates the all-eligible first round)
   a.mode = mode;
   a.m2 = d_match;
+  a.vgid = vgid;
+  a.gbase = gbase;
+  a.gcap = gcap;
   bool ok = true;
   auto take = [&](size_t bytes) {
     void *p = ws_take(ctx, bytes);

@@ -469,49 +469,21 @@ extern "C" void cm_part_default_params(cm_part_params *p) {
   p->coarsen_to = 0;
 }
 
-extern "C" int cm_part_graph(cm_ctx *ctx, int32_t nvtxs, const int32_t *xadj, const int32_t *adjncy,
-                             const int32_t *vwgt, const int32_t *adjwgt, int32_t nparts, const float *tpwgts,
-                             const float *ubvec, int32_t *objval, int32_t *part, const cm_part_params *params,
-                             cm_part_stats *stats) {
-  (void)tpwgts;  // accepted and ignored, as by the reference (cu:370-394)
-  (void)ubvec;
-  if (!ctx || nvtxs < 0 || !part || nparts < 1 || (nvtxs > 0 && (!xadj || xadj[nvtxs] < 0 || (xadj[nvtxs] > 0 && !adjncy))))
-    return cm_fail(CM_ERR_INVALID, "cm_part_graph: bad arguments");
-  cm_part_params P;
-  cm_part_default_params(&P);
-  if (params) P = *params;
-  const auto t_all = std::chrono::steady_clock::now();
-  cm_part_stats S{};
-  if (nvtxs == 0 || nparts == 1) {
-    for (int i = 0; i < nvtxs; ++i) part[i] = 0;
-    if (objval) *objval = 0;
-    if (stats) *stats = S;
-    return CM_OK;
-  }
+// Initial partition of the hierarchy's coarsest graph on the host, then per
+// level, coarsest to finest, projection and refinement on the context's
+// stream (cuMetis_kway_partition after cuMetis_coarsen, cu:3544-3616).  Takes
+// the hierarchy (frees it); part receives the finest level's partition.
+int part_hierarchy(cm_ctx *ctx, cm_hierarchy *h, int32_t nparts, const cm_part_params &P, int32_t *part,
+                   int32_t *objval, cm_part_stats *stats) {
+  cm_part_stats S = stats ? *stats : cm_part_stats{};
   int rc = set_device(ctx);
-  if (rc) return rc;
-  cudaStream_t s = ctx->stream;  // the context's own stream: concurrent contexts overlap
-  const int64_t m = xadj[nvtxs];
-  // Unit weights where the caller passes none (cuMetis_set_graph, cu:479-503).
-  std::vector<int32_t> uv, ue;
-  if (!vwgt) {
-    uv.assign(nvtxs, 1);
-    vwgt = uv.data();
+  if (rc) {
+    cm_hierarchy_free(h);
+    return rc;
   }
-  if (!adjwgt) {
-    ue.assign(std::max<int64_t>(m, 1), 1);
-    adjwgt = ue.data();
-  }
-  cm_graph hg{nvtxs, (int32_t)m, const_cast<int32_t *>(xadj), const_cast<int32_t *>(adjncy), const_cast<int32_t *>(adjwgt),
-              const_cast<int32_t *>(vwgt)};
-  cm_coarsen_params cp;
-  cm_coarsen_default_params(nvtxs, nparts, &cp);
-  if (P.coarsen_to > 0) cp.coarsen_to = P.coarsen_to;
-  cp.match_mode = P.match_mode;
-  cm_hierarchy *h = nullptr;
+  cudaStream_t s = ctx->stream;
+  const int32_t nvtxs = h->levels[0].g.nvtxs;
   auto t0 = std::chrono::steady_clock::now();
-  if ((rc = cm_coarsen(ctx, &hg, 0, &cp, &h, s))) return rc;
-  S.coarsen_ms = ms_since(t0);
   const int L = cm_hierarchy_levels(h);
   S.levels = L;
   std::vector<cm_graph> lg(L);
@@ -586,10 +558,58 @@ extern "C" int cm_part_graph(cm_ctx *ctx, int32_t nvtxs, const int32_t *xadj, co
   S.uncoarsen_ms = ms_since(t0);
   S.moves = (int64_t)moves;
   S.edge_cut = cut;
-  S.total_ms = ms_since(t_all);
   if (objval) *objval = (int32_t)cut;
   if (stats) *stats = S;
   return finish(CM_OK);
+}
+
+extern "C" int cm_part_graph(cm_ctx *ctx, int32_t nvtxs, const int32_t *xadj, const int32_t *adjncy,
+                             const int32_t *vwgt, const int32_t *adjwgt, int32_t nparts, const float *tpwgts,
+                             const float *ubvec, int32_t *objval, int32_t *part, const cm_part_params *params,
+                             cm_part_stats *stats) {
+  (void)tpwgts;  // accepted and ignored, as by the reference (cu:370-394)
+  (void)ubvec;
+  if (!ctx || nvtxs < 0 || !part || nparts < 1 || (nvtxs > 0 && (!xadj || xadj[nvtxs] < 0 || (xadj[nvtxs] > 0 && !adjncy))))
+    return cm_fail(CM_ERR_INVALID, "cm_part_graph: bad arguments");
+  cm_part_params P;
+  cm_part_default_params(&P);
+  if (params) P = *params;
+  const auto t_all = std::chrono::steady_clock::now();
+  cm_part_stats S{};
+  if (nvtxs == 0 || nparts == 1) {
+    for (int i = 0; i < nvtxs; ++i) part[i] = 0;
+    if (objval) *objval = 0;
+    if (stats) *stats = S;
+    return CM_OK;
+  }
+  int rc = set_device(ctx);
+  if (rc) return rc;
+  cudaStream_t s = ctx->stream;  // the context's own stream: concurrent contexts overlap
+  const int64_t m = xadj[nvtxs];
+  // Unit weights where the caller passes none (cuMetis_set_graph, cu:479-503).
+  std::vector<int32_t> uv, ue;
+  if (!vwgt) {
+    uv.assign(nvtxs, 1);
+    vwgt = uv.data();
+  }
+  if (!adjwgt) {
+    ue.assign(std::max<int64_t>(m, 1), 1);
+    adjwgt = ue.data();
+  }
+  cm_graph hg{nvtxs, (int32_t)m, const_cast<int32_t *>(xadj), const_cast<int32_t *>(adjncy), const_cast<int32_t *>(adjwgt),
+              const_cast<int32_t *>(vwgt)};
+  cm_coarsen_params cp;
+  cm_coarsen_default_params(nvtxs, nparts, &cp);
+  if (P.coarsen_to > 0) cp.coarsen_to = P.coarsen_to;
+  cp.match_mode = P.match_mode;
+  cm_hierarchy *h = nullptr;
+  auto t0 = std::chrono::steady_clock::now();
+  if ((rc = cm_coarsen(ctx, &hg, 0, &cp, &h, s))) return rc;
+  S.coarsen_ms = ms_since(t0);
+  rc = part_hierarchy(ctx, h, nparts, P, part, objval, &S);
+  S.total_ms = ms_since(t_all);
+  if (stats) *stats = S;
+  return rc;
 }
 
 // Drop-in with the reference's parameter list (include/cuMetis.h:18-19): one

@@ -174,6 +174,18 @@ class Context:
                                 _stream_ptr(stream)))
         return Hierarchy(h, keep=g)
 
+    def coarsen_batch(self, graphs, coarsen_to, mode=MATCH_HEM, maxvwgt=0, shrink=0.75, max_levels=64, stream=None):
+        """Coarsens host Graphs together (cm_coarsen_batch); coarsen_to is one
+        threshold or one per graph.  Returns one Hierarchy per graph."""
+        ng = len(graphs)
+        thr = list(coarsen_to) if hasattr(coarsen_to, "__len__") else [coarsen_to] * ng
+        gs = (cm_graph * max(ng, 1))(*[g.as_cm() for g in graphs])
+        ps = (cm_coarsen_params * max(ng, 1))(*[cm_coarsen_params(int(t), int(maxvwgt), int(mode), int(max_levels),
+                                                                   float(shrink)) for t in thr])
+        hs = (ctypes.c_void_p * max(ng, 1))()
+        _check(lib().cm_coarsen_batch(self._h, ng, gs, ps, hs, _stream_ptr(stream)))
+        return [Hierarchy(ctypes.c_void_p(hs[i]), keep=graphs[i]) for i in range(ng)]
+
 
 class Hierarchy:
     """Levels of one coarsening, resident on the device."""

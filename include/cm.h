@@ -249,6 +249,18 @@ int cm_hierarchy_copy_level(const cm_hierarchy *h, int32_t level, cm_graph *out,
 int cm_hierarchy_read_level(const cm_hierarchy *h, int32_t level, int32_t *xadj, int32_t *adjncy,
                             int32_t *adjwgt, int32_t *vwgt);
 
+/* Coarsens ngraphs host graphs together.  No counterpart in the reference
+ * (one graph per process).  Every level of all the graphs still coarsening
+ * is one graph of their disjoint union -- one matching launch and one
+ * contraction for all of them -- after which each graph's coarse level is
+ * split back into its own storage and each graph applies the stop rule
+ * (params[i]: its threshold, cap, tie order, level limit) on its own sizes.
+ * out[i] gets graph i's hierarchy, level for level the same as cm_coarsen
+ * of that graph alone.  Levels of different graphs share device
+ * allocations, which are released with their last hierarchy. */
+int cm_coarsen_batch(cm_ctx *ctx, int32_t ngraphs, const cm_graph *graphs_host,
+                     const cm_coarsen_params *params, cm_hierarchy **out, void *stream);
+
 /* ---- partitioning: the tail of cuMetis_PartGraph ------------------------ */
 
 /* Initial partition of a host graph (normally the coarsest level) by
