@@ -252,10 +252,12 @@ def run_batch(args):
     dt = time.perf_counter() - t1
     clk = clocks.stop()
     # The plain per-graph launch for comparison: one context, one graph at a
-    # time (cm_part_graph), on a sample of the same batch.
+    # time (cm_part_graph), on the same graphs (every one, or a sample with
+    # --plain-sample).
     import torch
     ctx1 = cm.Context(0)
-    sample = list(range(0, len(graphs), max(1, len(graphs) // 64)))
+    step_ = max(1, len(graphs) // args.plain_sample) if args.plain_sample > 0 else 1
+    sample = list(range(0, len(graphs), step_))
     for i in sample[:4]:
         ctx1.part_graph(graphs[i], ks[i])
     torch.cuda.synchronize()
@@ -278,12 +280,13 @@ def run_batch(args):
                        "description": "random geometric graphs, n log-uniform [1k,200k], mean degree 8, "
                                       "k uniform in {2..64} even, unit weights",
                        "workers": args.workers, "generation_s": gen_s, "engine_setup_ms": st["setup_ms"],
-                       "mean_phase_ms": {"coarsen": st["sum_coarsen_ms"] / len(graphs),
+                       "mean_phase_ms": {"coarsen_in_batch": st["sum_coarsen_ms"] / len(graphs),
                                          "initial_partition": st["sum_init_ms"] / len(graphs),
                                          "refine_project": st["sum_uncoarsen_ms"] / len(graphs)}},
             "edges_per_s": m_sum / dt, "mean_edge_cut": float(np.mean(cuts)),
             "plain_per_graph": {"partitions_per_s": plain_rate, "edges_per_s": sample_m / plain_dt,
-                                "sample_graphs": len(sample),
+                                "graphs": len(sample), "seconds": plain_dt,
+                                "batch_speedup_partitions": (len(graphs) / dt) / plain_rate,
                                 "batch_speedup_edges": (m_sum / dt) / (sample_m / plain_dt)},
             "mean_imbalance_first64": float(np.mean(imb)), "clocks": clk, "gpu_launches": None,
             "e2e": {"value": len(graphs) / dt, "unit": "partitions/s",
@@ -389,6 +392,8 @@ def main():
     ap.add_argument("--workload", default="rmat22", choices=sorted(WORKLOADS) + ["batch", "serve"])
     ap.add_argument("--workers", type=int, default=16, help="batch/serve: worker threads (one context each)")
     ap.add_argument("--batch-graphs", type=int, default=4096)
+    ap.add_argument("--plain-sample", type=int, default=0,
+                    help="batch: graphs of the plain per-graph comparison (0: every graph of the batch)")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: offered requests/s")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: arrival window in seconds")
     ap.add_argument("--serve-pool", type=int, default=48, help="serve: distinct request graphs")

@@ -25,8 +25,8 @@ CLI = os.path.join(HERE, "cuMetis")
 TUNED = os.path.join(HERE, "tuned.json")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["cm_ctx.cu", "cm_match.cu", "cm_cmap.cu", "cm_contract.cu", "cm_refine.cu", "cm_batch.cu"]
-CPP_SOURCES = ["cm_graph.cpp", "cm_initpart.cpp", "cm_engine.cpp"]
+CU_SOURCES = ["cm_ctx.cu", "cm_match.cu", "cm_cmap.cu", "cm_contract.cu", "cm_refine.cu", "cm_batch.cu", "cm_engine.cu"]
+CPP_SOURCES = ["cm_graph.cpp", "cm_initpart.cpp"]
 CLI_SOURCES = ["cm_cli.cpp"]
 
 

@@ -1,17 +1,19 @@
-// cm_engine.cpp -- many independent partitions on one GPU: the batched form
+// cm_engine.cu -- many independent partitions on one GPU: the batched form
 // (cm_part_batch) and the served form (cm_engine_*: submit / wait with
 // admission by device-memory footprint).  Neither has a counterpart in the
 // reference, which partitions one graph per process (cuMetis.cu:3874).
 //
-// Design: a pool of worker threads, each owning a cm_ctx (workspace, status
-// block, its own non-blocking stream).  A worker takes the oldest admitted
-// job and runs the whole pipeline for it (cm_part_graph: coarsening and
-// refinement on the worker's stream, the initial partition on the worker's
-// host thread).  Jobs of different workers overlap on the GPU through their
-// streams, and their host steps run in parallel on the host cores.  A job is
-// admitted while the estimated device memory of the running jobs stays within
-// the budget (a job larger than the budget runs alone).  Graphs are read from
-// the caller's host arrays, which must stay valid until the job is waited for.
+// Design: one scheduler thread owns a context and a batch coarsener.  Jobs
+// admitted by footprint join the batch before its next level; each level
+// coarsens every graph still coarsening in one set of launches (the graphs
+// laid side by side as one disjoint union, cm_batch.cu), and a graph whose
+// stop rule ends its coarsening leaves the batch at once -- continuous
+// batching at level granularity.  A pool of worker threads, each owning a
+// context and its own stream, then takes the coarsened jobs and runs the
+// rest of the pipeline (the initial partition on the worker's host thread,
+// projection and refinement on its stream), smallest coarsest graph first
+// unless a job has waited longer than kReadyAgeMs.  Graphs are read from the
+// caller's host arrays, which must stay valid until the job is waited for.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -25,6 +27,7 @@
 #include <vector>
 
 #include "cm.h"
+#include "cm_batch.h"
 #include "cm_internal.h"
 
 namespace {
@@ -47,9 +50,15 @@ struct Job {
   std::string error;
   cm_part_stats stats{};
   Clock::time_point t_submit, t_start, t_end;
+  Clock::time_point t_batch, t_coarsened;  // joined the batch / left it coarsened
+  cm_hierarchy *h = nullptr;               // its levels once coarsened
+  int32_t coarsest = 0;                    // vertices of its coarsest level
   bool done = false;
   bool waited = false;  // a thread is in cm_engine_wait for this job
 };
+
+// A coarsened job that waited this long is taken before smaller ones.
+constexpr double kReadyAgeMs = 250.0;
 
 // Device bytes a job holds while it runs: the level graphs (input and coarse
 // levels, each with match and cmap), the context workspace of the finest
@@ -64,12 +73,15 @@ struct cm_engine {
   int device = 0;
   int64_t budget = 0;
   int32_t max_queue = 0;       // <= 0: unbounded
-  std::vector<cm_ctx *> ctxs;
+  std::vector<cm_ctx *> ctxs;  // workers' contexts
+  cm_ctx *sched_ctx = nullptr; // the scheduler's context (batch coarsening)
   std::vector<std::thread> threads;
+  std::thread sched;
   std::mutex mu;
-  std::condition_variable cv_work, cv_done;
-  std::deque<Job *> pending;   // submitted, waiting for admission (FIFO)
-  std::deque<Job *> ready;     // admitted, waiting for a worker
+  std::condition_variable cv_work, cv_done, cv_sched;
+  std::deque<Job *> pending;   // submitted, waiting for admission (FIFO by footprint)
+  std::vector<Job *> admitted; // admitted, to join the batch before its next level
+  std::vector<Job *> ready;    // coarsened, waiting for a worker
   std::unordered_map<int64_t, std::unique_ptr<Job>> jobs;
   int64_t inflight = 0;        // footprint of admitted jobs not yet finished
   int64_t next_id = 1;
@@ -80,15 +92,114 @@ struct cm_engine {
   std::vector<double> latencies;
 
   void admit_locked() {
+    bool any = false;
     while (!pending.empty()) {
       Job *j = pending.front();
       const bool fits = budget <= 0 || inflight + j->footprint <= budget || inflight == 0;
       if (!fits) break;
       pending.pop_front();
       inflight += j->footprint;
-      ready.push_back(j);
-      cv_work.notify_one();
+      admitted.push_back(j);
+      any = true;
     }
+    if (any) cv_sched.notify_one();
+  }
+
+  void finish_locked(Job *j, int rc, const std::string &err) {
+    j->t_end = Clock::now();
+    j->status = rc;
+    j->error = err;
+    j->done = true;
+    inflight -= j->footprint;
+    ++completed;
+    latencies.push_back(ms_between(j->t_submit, j->t_end));
+    admit_locked();
+  }
+
+  // The next coarsened job for a worker: the oldest if it waited longer than
+  // kReadyAgeMs, else the one with the smallest coarsest graph.
+  Job *take_ready_locked() {
+    if (ready.empty()) return nullptr;
+    const auto now = Clock::now();
+    size_t pick = 0, oldest = 0;
+    for (size_t i = 1; i < ready.size(); ++i) {
+      if (ready[i]->t_coarsened < ready[oldest]->t_coarsened) oldest = i;
+      if (ready[i]->coarsest < ready[pick]->coarsest) pick = i;
+    }
+    if (ms_between(ready[oldest]->t_coarsened, now) > kReadyAgeMs) pick = oldest;
+    Job *j = ready[pick];
+    ready.erase(ready.begin() + pick);
+    return j;
+  }
+
+  void scheduler() {
+    auto B = std::make_unique<cm::BatchCoarsener>(sched_ctx, sched_ctx->stream);
+    std::unordered_map<int64_t, Job *> inbatch;
+    std::vector<std::pair<int64_t, cm_hierarchy *>> fin;
+    auto fail_all = [&](int rc) {
+      const std::string err = cm_last_error();
+      std::lock_guard<std::mutex> lk(mu);
+      for (auto &kv : inbatch) finish_locked(kv.second, rc, err);
+      inbatch.clear();
+      cv_done.notify_all();
+    };
+    for (;;) {
+      std::vector<Job *> add;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_sched.wait(lk, [&] { return stop || !admitted.empty() || !B->empty(); });
+        if (stop) break;
+        add.swap(admitted);
+      }
+      fin.clear();
+      int rc = CM_OK;
+      if (!add.empty()) {
+        std::vector<cm_graph> gs(add.size());
+        std::vector<cm_coarsen_params> ps(add.size());
+        std::vector<int64_t> tags(add.size());
+        const auto now = Clock::now();
+        for (size_t i = 0; i < add.size(); ++i) {
+          Job *j = add[i];
+          j->t_batch = now;
+          gs[i] = j->g;
+          cm_coarsen_default_params(j->g.nvtxs, j->nparts, &ps[i]);
+          if (j->params.coarsen_to > 0) ps[i].coarsen_to = j->params.coarsen_to;
+          ps[i].match_mode = j->params.match_mode;
+          tags[i] = j->id;
+          inbatch[j->id] = j;
+        }
+        rc = B->add((int32_t)add.size(), gs.data(), ps.data(), tags.data(), fin);
+      }
+      if (rc == CM_OK && !B->empty()) rc = B->step(fin);
+      if (rc == CM_OK) rc = cm::cuda_status(cudaStreamSynchronize(sched_ctx->stream), "batch level");
+      if (rc != CM_OK) {
+        for (auto &f : fin) cm_hierarchy_free(f.second);
+        fail_all(rc);
+        B = std::make_unique<cm::BatchCoarsener>(sched_ctx, sched_ctx->stream);  // frees what it held
+        continue;
+      }
+      if (fin.empty()) continue;
+      const auto now = Clock::now();
+      std::lock_guard<std::mutex> lk(mu);
+      for (auto &f : fin) {
+        Job *j = inbatch[f.first];
+        inbatch.erase(f.first);
+        j->h = f.second;
+        j->t_coarsened = now;
+        cm_graph cg{};
+        cm_hierarchy_level(j->h, cm_hierarchy_levels(j->h) - 1, &cg, nullptr, nullptr);
+        j->coarsest = cg.nvtxs;
+        ready.push_back(j);
+      }
+      cv_work.notify_all();
+    }
+    // shutting down: jobs still coarsening or admitted are dropped
+    B.reset();
+    std::lock_guard<std::mutex> lk(mu);
+    for (auto &kv : inbatch) finish_locked(kv.second, CM_ERR_INVALID, "cm_engine_wait: the engine was destroyed before the job ran");
+    for (Job *j : admitted) finish_locked(j, CM_ERR_INVALID, "cm_engine_wait: the engine was destroyed before the job ran");
+    admitted.clear();
+    cv_done.notify_all();
   }
 
   void worker(int w) {
@@ -98,28 +209,31 @@ struct cm_engine {
       {
         std::unique_lock<std::mutex> lk(mu);
         cv_work.wait(lk, [&] { return stop || !ready.empty(); });
-        if (ready.empty()) return;  // stop requested and nothing left
-        j = ready.front();
-        ready.pop_front();
+        if (stop && ready.empty()) return;
+        j = take_ready_locked();
+        if (!j) continue;
         j->t_start = Clock::now();
       }
       int32_t obj = 0;
       cm_part_stats st{};
-      const int rc = cm_part_graph(ctx, j->g.nvtxs, j->g.xadj, j->g.adjncy, j->g.vwgt, j->g.adjwgt, j->nparts,
-                                   nullptr, nullptr, &obj, j->part, &j->params, &st);
+      st.coarsen_ms = ms_between(j->t_batch, j->t_coarsened);
+      cm_hierarchy *h = j->h;
+      j->h = nullptr;
+      h->stream = ctx->stream;  // frees of its own blocks and waits go to this worker's stream
+      int rc = CM_OK;
+      if (j->nparts == 1 || h->levels[0].g.nvtxs == 0) {
+        for (int i = 0; i < h->levels[0].g.nvtxs; ++i) j->part[i] = 0;
+        cm_hierarchy_free(h);
+      } else {
+        rc = part_hierarchy(ctx, h, j->nparts, j->params, j->part, &obj, &st);
+      }
+      st.total_ms = ms_between(j->t_batch, Clock::now());
       std::string err = rc == CM_OK ? std::string() : std::string(cm_last_error());
       {
         std::lock_guard<std::mutex> lk(mu);
-        j->t_end = Clock::now();
-        j->status = rc;
-        j->error = err;
         j->objval = obj;
         j->stats = st;
-        j->done = true;
-        inflight -= j->footprint;
-        ++completed;
-        latencies.push_back(ms_between(j->t_submit, j->t_end));
-        admit_locked();
+        finish_locked(j, rc, err);
       }
       cv_done.notify_all();
     }
@@ -145,7 +259,15 @@ extern "C" int cm_engine_create(int device, int32_t nworkers, int64_t hbm_budget
     }
     e->ctxs.push_back(c);
   }
+  int rc = cm_ctx_create(device, &e->sched_ctx);
+  if (rc == CM_OK && (reserve_nvtxs > 0 || reserve_nedges > 0)) rc = cm_ctx_reserve(e->sched_ctx, reserve_nvtxs, reserve_nedges);
+  if (rc != CM_OK) {
+    if (e->sched_ctx) cm_ctx_destroy(e->sched_ctx);
+    for (cm_ctx *x : e->ctxs) cm_ctx_destroy(x);
+    return rc;
+  }
   cm_engine *raw = e.get();
+  e->sched = std::thread([raw] { raw->scheduler(); });
   for (int w = 0; w < nworkers; ++w) e->threads.emplace_back([raw, w] { raw->worker(w); });
   *out = e.release();
   return CM_OK;
@@ -174,6 +296,8 @@ extern "C" void cm_engine_destroy(cm_engine *e) {
   }
   e->cv_work.notify_all();
   e->cv_done.notify_all();
+  e->cv_sched.notify_all();
+  e->sched.join();
   for (auto &t : e->threads) t.join();
   {
     // threads still inside cm_engine_wait leave before the engine goes away
@@ -181,6 +305,7 @@ extern "C" void cm_engine_destroy(cm_engine *e) {
     e->cv_done.wait(lk, [&] { return e->waiters == 0; });
   }
   for (cm_ctx *c : e->ctxs) cm_ctx_destroy(c);
+  cm_ctx_destroy(e->sched_ctx);
   delete e;
 }
 

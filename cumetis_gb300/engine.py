@@ -1,5 +1,5 @@
 """Batched and served partitioning: Python side of cm_engine_* and
-cm_part_batch (the worker pool lives in libcm, cm_engine.cpp)."""
+cm_part_batch (the scheduler and worker pool live in libcm, cm_engine.cu)."""
 import ctypes
 
 import numpy as np
