@@ -311,18 +311,14 @@ def serve_pool(seed=1, count=48):
     return pool
 
 
-def run_serve(args):
-    """Served partitioning (cm_engine): Poisson arrivals at --rate requests/s
-    for --duration seconds, each a random pool graph with k uniform in
-    {8..256}.  Submissions beyond --max-queue waiting jobs are rejected; after
-    the window the engine drains for at most --drain seconds, then drops what
-    has not started.  Reports completions/s and latency percentiles of the
-    completed requests."""
+def serve_once(args, pool, rate, duration, drain, seed=7):
+    """One served run: Poisson arrivals at `rate` requests/s for `duration`
+    seconds, each a random pool graph with k uniform in {8..256};
+    submissions beyond --max-queue waiting jobs are rejected; after the window
+    the engine drains for at most `drain` seconds, then drops what has not
+    finished.  Returns the run's counts and latency percentiles."""
     import cumetis_gb300 as cm
-    rng = np.random.default_rng(7)
-    t0 = time.perf_counter()
-    pool = serve_pool(count=args.serve_pool)
-    gen_s = time.perf_counter() - t0
+    rng = np.random.default_rng(seed)
     max_n = max(g.nvtxs for _, g in pool)
     max_m = max(g.nedges for _, g in pool)
     eng = cm.Engine(0, workers=args.workers, hbm_budget_bytes=int(args.hbm_budget_gb * 2**30),
@@ -330,14 +326,12 @@ def run_serve(args):
     for _, g in pool[:4]:  # warm-up
         eng.wait(eng.submit(g, 16))
     eng.stats(reset=True)
-    clocks = ClockSampler(0)
-    clocks.start()
     jobs, rejected = [], 0
     t_start = time.perf_counter()
     t_next = t_start
     while True:
         now = time.perf_counter()
-        if now - t_start >= args.duration:
+        if now - t_start >= duration:
             break
         if now < t_next:
             time.sleep(min(t_next - now, 0.001))
@@ -349,9 +343,8 @@ def run_serve(args):
             if e.code != cm.CM_ERR_LIMIT:
                 raise
             rejected += 1
-        t_next += rng.exponential(1.0 / args.rate)
-    t_window = time.perf_counter()
-    deadline = t_window + args.drain
+        t_next += rng.exponential(1.0 / rate)
+    deadline = time.perf_counter() + drain
     lat, unfinished = [], 0
     for j in jobs:
         while not eng.poll(j) and time.perf_counter() < deadline:
@@ -361,24 +354,53 @@ def run_serve(args):
         else:
             unfinished += 1
     t_end = time.perf_counter()
-    clk = clocks.stop()
-    eng.close()  # drops jobs that never started
+    eng.close()  # drops jobs that never finished
     lat = np.sort(np.array(lat))
     done = len(lat)
-    line = {"metric": "partitions/s", "value": done / (t_end - t_start), "unit": "partitions/s", "n_gpus": 1,
-            "steps": done, "warmup": 4, "ms_per_step": (t_end - t_start) * 1e3 / max(done, 1),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": "serve", "offered_rate": args.rate, "duration_s": args.duration,
-                       "drain_s": args.drain, "max_queue": args.max_queue, "pool": len(pool),
-                       "pool_generation_s": gen_s, "workers": args.workers, "hbm_budget_gb": args.hbm_budget_gb,
-                       "description": "Poisson arrivals; 50% 3D 7-point grids side U[20,120], 50% R-MAT "
-                                      "s14-21 (ef 16, weights U[1,100]); k uniform in {8..256}"},
-            "submitted": len(jobs), "rejected": rejected, "completed": done, "unfinished_dropped": unfinished,
+    offered = len(jobs) + rejected
+    return {"offered_rate": rate, "offered": offered, "rejected": rejected, "unfinished_dropped": unfinished,
+            "completed": done, "failed_frac": (rejected + unfinished) / max(offered, 1),
+            "partitions_per_s": done / (t_end - t_start), "seconds": t_end - t_start,
             "latency_ms": {"p50": float(np.percentile(lat, 50)) if done else None,
                            "p99": float(np.percentile(lat, 99)) if done else None,
-                           "max": float(lat[-1]) if done else None},
-            "clocks": clk, "gpu_launches": None,
-            "e2e": {"value": done / (t_end - t_start), "unit": "partitions/s", "h2d_bytes_per_step": None,
+                           "max": float(lat[-1]) if done else None}}
+
+
+def run_serve(args):
+    """Served partitioning (cm_engine) at --rate requests/s; with
+    --serve-rates, a sweep of offered rates (ascending, stopping at the first
+    rate where 1% or more of the requests were rejected or not finished),
+    reporting the highest rate served within that bound and the run at
+    --rate beside it."""
+    t0 = time.perf_counter()
+    pool = serve_pool(count=args.serve_pool)
+    gen_s = time.perf_counter() - t0
+    clocks = ClockSampler(0)
+    clocks.start()
+    sweep = []
+    if args.serve_rates:
+        for r in [float(x) for x in args.serve_rates.split(",")]:
+            res = serve_once(args, pool, r, args.duration, args.drain)
+            sweep.append(res)
+            if res["failed_frac"] >= 0.01:
+                break
+    main_run = serve_once(args, pool, args.rate, args.duration, args.drain)
+    clk = clocks.stop()
+    ok = [r for r in sweep if r["failed_frac"] < 0.01]
+    best = max(ok, key=lambda r: r["offered_rate"]) if ok else None
+    head = best or main_run
+    line = {"metric": "partitions/s", "value": head["partitions_per_s"], "unit": "partitions/s", "n_gpus": 1,
+            "steps": head["completed"], "warmup": 4, "ms_per_step": head["seconds"] * 1e3 / max(head["completed"], 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": "serve", "duration_s": args.duration, "drain_s": args.drain,
+                       "max_queue": args.max_queue, "pool": len(pool), "pool_generation_s": gen_s,
+                       "workers": args.workers, "hbm_budget_gb": args.hbm_budget_gb,
+                       "description": "Poisson arrivals; 50% 3D 7-point grids side U[20,120], 50% R-MAT "
+                                      "s14-21 (ef 16, weights U[1,100]); k uniform in {8..256}"},
+            "max_rate_under_1pct_failed": best["offered_rate"] if best else None,
+            "at_max_rate": best, "at_offered_rate": main_run, "sweep": sweep,
+            "latency_ms": head["latency_ms"], "clocks": clk, "gpu_launches": None,
+            "e2e": {"value": head["partitions_per_s"], "unit": "partitions/s", "h2d_bytes_per_step": None,
                     "d2h_bytes_per_step": None}}
     print(json.dumps(line), flush=True)
 
@@ -395,6 +417,7 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=0,
                     help="batch: graphs of the plain per-graph comparison (0: every graph of the batch)")
     ap.add_argument("--rate", type=float, default=2000.0, help="serve: offered requests/s")
+    ap.add_argument("--serve-rates", default="", help="serve: offered rates to sweep, e.g. 1,2,5,10,20")
     ap.add_argument("--duration", type=float, default=10.0, help="serve: arrival window in seconds")
     ap.add_argument("--serve-pool", type=int, default=48, help="serve: distinct request graphs")
     ap.add_argument("--hbm-budget-gb", type=float, default=200.0, help="serve: admission budget")
