@@ -220,7 +220,7 @@ int BatchCoarsener::step(std::vector<std::pair<int64_t, cm_hierarchy *>> &finish
   if (rc) return rc;
   // Groups: one tie order per union, sizes within the int32 CSR limits.
   std::vector<std::vector<int>> groups;
-  for (int mode : {CM_MATCH_HEM, CM_MATCH_HEM_HASH}) {
+  for (int mode : {CM_MATCH_HEM, CM_MATCH_HEM_HASH, CM_MATCH_RACY}) {
     std::vector<int> cur;
     int64_t N = 0, M = 0;
     for (int i = 0; i < (int)active_.size(); ++i) {

@@ -736,6 +736,79 @@ __global__ void k_match_finish(int n, int *__restrict__ m2) {
     if (m2[v] < 0) m2[v] = (int)v;
 }
 
+// ---------------------------------------------------------------------------
+// CM_MATCH_RACY: one unsynchronised proposal pass and its cleanup, as the
+// reference's cuda_shem2 (cu:1563-1595) + cuda_cleanv (cu:1600) + findc1
+// (cu:1621).  A light vertex (3 vwgt < cap) that nobody has claimed takes,
+// among its neighbours that already point at it or are unmatched within the
+// weight cap, the heaviest one (the reference walks its row sorted by weight,
+// heaviest first, and stops at the first such neighbour), and writes both
+// ends with plain stores; concurrent writers race.  The cleanup then turns
+// every vertex whose partner does not point back into a singleton.  The
+// result is a legal matching, not a maximal one, and depends on the schedule.
+// One warp per vertex (the reference uses one thread per vertex).
+// ---------------------------------------------------------------------------
+constexpr int kRacyThreads = 256;
+
+__global__ void k_racy_init(int n, int *__restrict__ m) {
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x)
+    m[v] = -1;
+}
+
+__global__ void __launch_bounds__(kRacyThreads) k_racy_propose(MatchArgs a) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (kRacyThreads / 32);
+  volatile int *m = a.m2;
+  for (long long v = (long long)blockIdx.x * (kRacyThreads / 32) + (threadIdx.x >> 5); v < a.n; v += warps) {
+    const long long cap = weight_cap(a, (int)v);
+    const long long vw = a.vwgt[v];
+    if (!(3 * vw < cap)) continue;
+    if (m[v] != -1) continue;  // already claimed
+    // heaviest candidate; equal weights by the edge hash (both ends of an
+    // edge rank it alike, which the reference's unstable weight sort leaves
+    // to chance)
+    const int hb = hash_base(a, (int)v);
+    int bw = INT_MIN, bk = -1;
+    unsigned bh = 0xffffffffu;
+    for (int j = a.xadj[v] + lane; j < a.xadj[v + 1]; j += 32) {
+      const int k = a.adjncy[j];
+      if (k == v) continue;
+      const int mk = m[k];
+      const bool ok = mk == (int)v || (mk == -1 && vw + a.vwgt[k] <= cap);
+      if (!ok) continue;
+      const int w = a.adjwgt[j];
+      const unsigned h = edge_hash((unsigned)(min((int)v, k) - hb), (unsigned)(max((int)v, k) - hb));
+      if (w > bw || (w == bw && h < bh)) {
+        bw = w;
+        bh = h;
+        bk = k;
+      }
+    }
+    const int top = __reduce_max_sync(0xffffffffu, bk >= 0 ? bw : INT_MIN);
+    const unsigned hmin = __reduce_min_sync(0xffffffffu, (bk >= 0 && bw == top) ? bh : 0xffffffffu);
+    const unsigned holders = __ballot_sync(0xffffffffu, bk >= 0 && bw == top && bh == hmin);
+    if (holders == 0) continue;
+    const int k = __shfl_sync(0xffffffffu, bk, __ffs(holders) - 1);
+    if (lane == 0 && m[v] == -1) {
+      m[v] = k;
+      if (m[k] != (int)v) m[k] = (int)v;
+    }
+  }
+}
+
+// s[v] = 1 if v keeps its partner (unmatched, or the partner points back).
+__global__ void k_racy_clean(int n, const int *__restrict__ m, int *__restrict__ s) {
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x) {
+    const int u = m[v];
+    s[v] = (u == -1 || m[u] == (int)v) ? 1 : 0;
+  }
+}
+
+__global__ void k_racy_apply(int n, int *__restrict__ m, const int *__restrict__ s) {
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < n; v += (long long)gridDim.x * blockDim.x)
+    if (s[v] == 0 || m[v] == -1) m[v] = (int)v;
+}
+
 int64_t max_chunks(int64_t n, int64_t m) { return m / kChunk + n + 64; }
 
 }  // namespace
@@ -752,8 +825,31 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
                  const int32_t *vgid, const int32_t *gbase, const int32_t *gcap) {
   const int n = g->nvtxs;
   if (n == 0) return CM_OK;
-  if (mode != CM_MATCH_HEM && mode != CM_MATCH_HEM_HASH)
-    return cm_fail(CM_ERR_UNSUPPORTED, "cm_match: mode %d not available", mode);
+  if (mode != CM_MATCH_HEM && mode != CM_MATCH_HEM_HASH && mode != CM_MATCH_RACY)
+    return cm_fail(CM_ERR_INVALID, "cm_match: unknown mode %d", mode);
+  if (mode == CM_MATCH_RACY) {
+    MatchArgs a{};
+    a.n = n;
+    a.xadj = g->xadj; a.adjncy = g->adjncy; a.adjwgt = g->adjwgt; a.vwgt = g->vwgt;
+    a.maxvwgt = maxvwgt;
+    a.m2 = d_match;
+    a.vgid = vgid;
+    a.gbase = gbase;
+    a.gcap = gcap;
+    int *flags = (int *)ws_take(ctx, (size_t)n * 4);
+    if (!flags) return cm_fail(CM_ERR_NOMEM, "cm_match: workspace too small");
+    const unsigned vg = (unsigned)std::min<int64_t>((int64_t)ctx->num_sms * 8, n / 256 + 1);
+    const unsigned wg = (unsigned)std::min<int64_t>((int64_t)ctx->num_sms * 16, n / (kRacyThreads / 32) + 1);
+    stage_begin(ctx, s);
+    k_racy_init<<<vg, 256, 0, s>>>(n, d_match);
+    k_racy_propose<<<wg, kRacyThreads, 0, s>>>(a);
+    k_racy_clean<<<vg, 256, 0, s>>>(n, d_match, flags);
+    k_racy_apply<<<vg, 256, 0, s>>>(n, d_match, flags);
+    stage_end(ctx, CM_STAGE_MATCH, s);
+    ctx->launches += 4;
+    cudaMemsetAsync(&ctx->d_status->rounds, 0, sizeof(int), s);
+    return check_launch(ctx, "cm_match (racy)");
+  }
   const int64_t ch = max_chunks(n, g->nedges);
   MatchArgs a;
   a.n = n;

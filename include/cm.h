@@ -59,8 +59,12 @@ enum {
   /* Same, but equal weights are ordered by a fixed hash of the edge's
    * endpoints (fewer handshake rounds on unit-weight meshes). */
   CM_MATCH_HEM_HASH = 1,
-  /* One unsynchronised proposal pass plus cleanup, like cuMetis.cu:1563-1630;
-   * nondeterministic, always a legal matching. */
+  /* One unsynchronised proposal pass plus cleanup, like cuMetis.cu:1563-1630
+   * (cuda_shem2, cuda_cleanv, findc1): a light vertex that nobody claimed
+   * takes its heaviest neighbour that points at it or is unmatched within
+   * the cap, with plain stores; vertices whose partner does not point back
+   * become singletons.  Nondeterministic, always a legal matching, not
+   * necessarily maximal. */
   CM_MATCH_RACY = 2
 };
 

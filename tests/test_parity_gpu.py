@@ -417,3 +417,31 @@ def test_rmat22_full_size(ctx):
     wcg, wcmap = O.contract(og, want)
     assert np.array_equal(cmap.cpu().numpy(), wcmap)
     assert_same_graph(_o(h), wcg, "rmat22")
+
+
+def test_racy_matching_is_legal_and_coarsens_like_the_reference(ctx, graphs):
+    """CM_MATCH_RACY (one unsynchronised proposal pass and its cleanup, the
+    reference's cuda_shem2 + cuda_cleanv + findc1): the result depends on the
+    schedule, so it is checked as a legal matching (involution, adjacent
+    partners, weight cap, a light proposer) on every graph, and its
+    coarsening ratio n'/n is compared with the reference's own CPU heavy-edge
+    matching on the golden graphs (seeds 1 and 2)."""
+    for name, g in graphs.items():
+        for mv in (O.maxvwgt_rule(int(g.vwgt.sum()), 100), 29):
+            for _ in range(2):
+                got, _ = gpu_match(ctx, g, mv, cm.MATCH_RACY)
+                code, bad, _ = O.check_matching(g, mv, got)
+                assert code == 0, (name, mv, code, bad)
+    for name in GOLDEN_CASES:
+        G = load_golden(name)
+        for seed, (maxvwgt, lv, cmaps) in G["seeds"].items():
+            g = lv[0]
+            ref_ratio = (int(cmaps[0].max()) + 1) / g.n
+            got, _ = gpu_match(ctx, g, maxvwgt, cm.MATCH_RACY)
+            assert O.check_matching(g, maxvwgt, got)[0] == 0, (name, seed)
+            ratio = (int(np.sum(got >= np.arange(g.n)))) / g.n
+            # pairs formed (1 - n'/n) against the reference's maximal CPU
+            # matching: one racy pass loses the pairs of its collisions
+            pairs, ref_pairs = 1.0 - ratio, 1.0 - ref_ratio
+            assert 0.3 * ref_pairs <= pairs <= 1.1 * ref_pairs, (name, seed, ratio, ref_ratio)
+            print("racy %s seed %d: n'/n %.3f, reference CPU matching %.3f" % (name, seed, ratio, ref_ratio))
