@@ -136,13 +136,11 @@ template <> struct Cand<false> {
     r.key = ((unsigned long long)hi << 32) | lo;
     return r;
   }
-  __device__ __forceinline__ void store(int *p) const {
-    p[0] = (int)(unsigned)(key >> 32);
-    p[1] = (int)(unsigned)key;
-  }
+  // p: 16-byte aligned slot of kPartInts ints
+  __device__ __forceinline__ void store(int *p) const { *reinterpret_cast<unsigned long long *>(p) = key; }
   __device__ __forceinline__ static Cand load(const int *p) {
     Cand c;
-    c.key = ((unsigned long long)(unsigned)__ldcg(p) << 32) | (unsigned)__ldcg(p + 1);
+    c.key = __ldcg(reinterpret_cast<const unsigned long long *>(p));
     return c;
   }
 };
@@ -180,20 +178,17 @@ template <> struct Cand<true> {
     r.k = kmin == 0xffffffffu ? INT_MAX : (int)kmin;
     return r;
   }
-  __device__ __forceinline__ void store(int *p) const {
-    p[0] = w;
-    p[1] = (int)h;
-    p[2] = k;
-  }
+  __device__ __forceinline__ void store(int *p) const { *reinterpret_cast<int4 *>(p) = make_int4(w, (int)h, k, 0); }
   __device__ __forceinline__ static Cand load(const int *p) {
+    const int4 x = __ldcg(reinterpret_cast<const int4 *>(p));
     Cand c;
-    c.w = __ldcg(p);
-    c.h = (unsigned)__ldcg(p + 1);
-    c.k = __ldcg(p + 2);
+    c.w = x.x;
+    c.h = (unsigned)x.y;
+    c.k = x.z;
     return c;
   }
 };
-constexpr int kPartInts = 3;  // ints per stored candidate (lex mode uses 2)
+constexpr int kPartInts = 4;  // ints per stored candidate slot (16 bytes, one vector access)
 
 // Sorted (best first) list of up to KK candidates held in registers.
 template <bool H, int KK>
@@ -252,6 +247,25 @@ __device__ __forceinline__ TopK<H, KK> warp_topk(const TopK<H, KK> &t) {
   return out;
 }
 
+// The warp's best KK of the cnt candidates stored at slots slot(t), t < cnt,
+// of the chunk partial lists (four loads in flight per lane).
+template <bool H, int KK, typename F>
+__device__ __forceinline__ TopK<H, KK> merge_parts(const MatchArgs &a, int cnt, F slot) {
+  const int lane = threadIdx.x & 31;
+  TopK<H, KK> acc;
+  for (int t0 = lane; t0 < cnt; t0 += 128) {
+    Cand<H> c[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int t = t0 + 32 * i;
+      if (t < cnt) c[i] = Cand<H>::load(a.part + slot(t) * kPartInts);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc.insert(c[i]);
+  }
+  return warp_topk(acc);
+}
+
 // Per-lane best KK over entries [b, e) (e - b <= kChunk) of v's row; all loads
 // of the chunk are issued before any is used.
 template <bool H, int KK>
@@ -259,22 +273,161 @@ __device__ __forceinline__ TopK<H, KK> lane_scan(const MatchArgs &a, int v, long
                                                  bool all_elig = false) {
   const int lane = threadIdx.x & 31;
   constexpr int U = kChunk / 32;
+  const int nu = (e - b + 31) >> 5;  // slots holding entries (warp-uniform): the others are skipped
   int k[U], w[U], s[U];
 #pragma unroll
   for (int u = 0; u < U; ++u) {
     const int j = b + lane + 32 * u;
-    k[u] = j < e ? a.adjncy[j] : -1;
-    w[u] = j < e ? a.adjwgt[j] : 0;
+    k[u] = -1;
+    w[u] = 0;
+    if (u < nu && j < e) {
+      k[u] = a.adjncy[j];
+      w[u] = a.adjwgt[j];
+    }
   }
 #pragma unroll
-  for (int u = 0; u < U; ++u) s[u] = (k[u] >= 0 && !all_elig) ? __ldcg(a.m2 + k[u]) : -1;
+  for (int u = 0; u < U; ++u) s[u] = (u < nu && k[u] >= 0 && !all_elig) ? __ldcg(a.m2 + k[u]) : -1;
   TopK<H, KK> t;
   const int hb = hash_base(a, v);
 #pragma unroll
   for (int u = 0; u < U; ++u)
-    if (k[u] >= 0 && (all_elig ? k[u] != v : eligible<H>(a, vw, v, k[u], s[u])))
+    if (u < nu && k[u] >= 0 && (all_elig ? k[u] != v : eligible<H>(a, vw, v, k[u], s[u])))
       t.insert_edge(v, k[u], w[u], hb);
   return t;
+}
+
+// Inserts x into the descending list tw (the KK largest values seen, with
+// repeats).
+template <int KK>
+__device__ __forceinline__ void wlist_insert(int (&tw)[KK], int x) {
+#pragma unroll
+  for (int i = 0; i < KK; ++i) {
+    const int hi = max(tw[i], x);
+    x = min(tw[i], x);
+    tw[i] = hi;
+  }
+}
+
+// The warp's best KK candidates over entries [b, e) (e - b <= kChunk) of v's
+// row; every lane gets the list.  Hash order: most entries are lighter than
+// the chunk's KK-th heaviest eligible entry and can never enter the list, so
+// a weight threshold W is found first and only entries of weight >= W get an
+// edge hash and a full comparison.  W is the KK-th largest weight of the
+// union of the lanes' own KK heaviest (a sub-multiset of the chunk), so at
+// least KK entries weigh >= W and the chunk's best KK are all among them.
+// The qualifying entries (usually KK plus the ties at W) are packed one per
+// lane through the warp's 32-entry buffer wbuf; more than 32 of them (many
+// equal weights) take the per-lane lists instead.
+template <bool H, int KK>
+__device__ __forceinline__ TopK<H, KK> chunk_best(const MatchArgs &a, int v, long long vw, int b, int e, bool all_elig,
+                                                  int2 *wbuf) {
+  if constexpr (!H) {
+    (void)wbuf;
+    return warp_topk(lane_scan<H, KK>(a, v, vw, b, e, all_elig));
+  } else {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    constexpr int U = kChunk / 32;
+    const int nu = (e - b + 31) >> 5;  // slots holding entries (warp-uniform): the others are skipped
+    int k[U], w[U], s[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int j = b + lane + 32 * u;
+      k[u] = -1;
+      w[u] = 0;
+      if (u < nu && j < e) {
+        k[u] = a.adjncy[j];
+        w[u] = a.adjwgt[j];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) s[u] = (u < nu && k[u] >= 0 && !all_elig) ? __ldcg(a.m2 + k[u]) : -1;
+    // k[u] = -1 marks an entry that is not an eligible candidate
+    int tw[KK], rem = 0;
+#pragma unroll
+    for (int i = 0; i < KK; ++i) tw[i] = INT_MIN;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (u >= nu) break;
+      if (k[u] >= 0 && !(all_elig ? k[u] != v : eligible<H>(a, vw, v, k[u], s[u]))) k[u] = -1;
+      if (k[u] >= 0) {
+        wlist_insert(tw, w[u]);
+        ++rem;
+      }
+    }
+    rem = min(rem, KK);
+    // threshold: pop the lanes' list heads in descending order until KK
+    // entries are taken (or every list is empty: then all eligible entries
+    // qualify, W being the lightest of them)
+    int W = INT_MIN, taken = 0;
+#pragma unroll
+    for (int r = 0; r < KK; ++r) {
+      const bool has = rem > 0;
+      if (!__ballot_sync(full, has)) break;
+      const int mine = has ? tw[0] : INT_MIN;
+      const int mx = __reduce_max_sync(full, mine);
+      const bool pop = has && mine == mx;
+      taken += __popc(__ballot_sync(full, pop));
+      W = mx;
+      if (pop) {
+#pragma unroll
+        for (int i = 0; i + 1 < KK; ++i) tw[i] = tw[i + 1];
+        --rem;
+      }
+      if (taken >= KK) break;
+    }
+    int total = 0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (u >= nu) break;
+      total += __popc(__ballot_sync(full, k[u] >= 0 && w[u] >= W));
+    }
+    const int hb = hash_base(a, v);
+    TopK<H, KK> out;
+    if (total > 32) {
+      TopK<H, KK> t;
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (u < nu && k[u] >= 0 && w[u] >= W) t.insert_edge(v, k[u], w[u], hb);
+      out = warp_topk(t);
+    } else {
+      const unsigned below = (1u << lane) - 1u;
+      int base = 0;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        if (u >= nu) break;
+        const bool q = k[u] >= 0 && w[u] >= W;
+        const unsigned bal = __ballot_sync(full, q);
+        if (q) wbuf[base + __popc(bal & below)] = make_int2(k[u], w[u]);
+        base += __popc(bal);
+      }
+      __syncwarp();
+      Cand<H> mine;
+      if (lane < total) {
+        const int2 x = wbuf[lane];
+        mine = Cand<H>::make(v, x.x, x.y, hb);
+      }
+      __syncwarp();  // the buffer is free for the warp's next chunk
+#pragma unroll
+      for (int i = 0; i < KK; ++i) {
+        const Cand<H> win = mine.warp_best();
+        out.c[i] = win;
+        if (win.valid() && mine.same(win)) mine = Cand<H>();
+      }
+    }
+    // Identical entries (parallel edges of equal weight) count once in the
+    // list but each in `taken`: a list left short although lighter entries
+    // exist is recomputed over every eligible entry, so that a short list
+    // still means "no other candidate".
+    if (taken >= KK && !out.c[KK - 1].valid()) {
+      TopK<H, KK> t;
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (u < nu && k[u] >= 0) t.insert_edge(v, k[u], w[u], hb);
+      out = warp_topk(t);
+    }
+    return out;
+  }
 }
 
 // Writes v's cached candidate ids and points v at the first.  A first scan
@@ -307,6 +460,25 @@ __device__ __forceinline__ void warp_append(int *list, int *counter, bool take, 
   if (take) list[base + __popc(mask & ((1u << lane) - 1))] = x;
 }
 
+// Chunk descriptors of the rows queued by the lanes with `take` set (row x of
+// deg entries from xs, nch chunks from desc[cb], row index idx): a one-chunk
+// row's lane writes its descriptor, and the warp writes each longer row's
+// descriptors together.  Convergent.
+__device__ __forceinline__ void write_descs(int4 *desc, bool take, int x, int xs, int deg, int nch, int idx, int cb) {
+  const int lane = threadIdx.x & 31;
+  if (take && nch == 1) desc[cb] = make_int4(x, xs, xs + deg, -1);
+  unsigned bm = __ballot_sync(0xffffffffu, take && nch > 1);
+  while (bm) {
+    const int src = __ffs(bm) - 1;
+    bm &= bm - 1;
+    const int rx = __shfl_sync(0xffffffffu, x, src), rs = __shfl_sync(0xffffffffu, xs, src);
+    const int rd = __shfl_sync(0xffffffffu, deg, src), rn = __shfl_sync(0xffffffffu, nch, src);
+    const int ri = __shfl_sync(0xffffffffu, idx, src), rc = __shfl_sync(0xffffffffu, cb, src);
+    for (int j = lane; j < rn; j += 32)
+      desc[rc + j] = make_int4(rx, rs + j * kChunk, min(rs + rd, rs + (j + 1) * kChunk), ri);
+  }
+}
+
 // Queues x (row of `deg` entries starting at xs) for a full scan in slot
 // `par`; convergent.
 __device__ __forceinline__ void append_scan(const MatchArgs &a, int par, bool take, int x, int xs, int deg) {
@@ -322,34 +494,109 @@ __device__ __forceinline__ void append_scan(const MatchArgs &a, int par, bool ta
   unsigned long long base = 0;
   if (lane == 0) base = atomicAdd(a.big + par, tot);
   base = __shfl_sync(0xffffffffu, base, 0) + ex;
+  const int idx = (int)(base >> 32), cb = (int)(base & 0xffffffffu);
   if (bg) {
-    const int idx = (int)(base >> 32), cb = (int)(base & 0xffffffffu);
     S.big_v[idx] = x;
     S.big_base[idx] = cb;
     S.big_done[idx] = 0;
-    for (int j = 0; j < nch; ++j)
-      S.desc[cb + j] = make_int4(x, xs + j * kChunk, min(xs + deg, xs + (j + 1) * kChunk), nch > 1 ? idx : -1);
   }
+  write_descs(S.desc, bg, x, xs, deg, nch, idx, cb);
 }
 
-// Block-aggregated append: every thread offers up to kCU items per list; one
-// atomicAdd per block and list.  All threads of the block must call it.
 constexpr int kCU = 4;  // vertices per thread in phase C
-__device__ __forceinline__ void block_append(int *list, int *counter, const bool (&take)[kCU], const int (&x)[kCU],
-                                             int *sh_scan, int *sh_base) {
-  int cnt = 0;
+
+// Phase C's appends for a block (all threads call it): every thread offers
+// up to kCU vertices to the next round's active list (keep), cache-update
+// list (upd) and scan lists (scan: the short-row list or, for longer rows,
+// the chunk list with one descriptor per kChunk entries).  One block-wide
+// scan of the packed per-thread counts (four 16-bit fields, block totals
+// <= kMatchThreads * kCU) and of the chunk counts, then one atomicAdd per
+// list, issued side by side by four lanes.
+static_assert(kMatchThreads * kCU < 65536, "phase C counts are packed in 16-bit fields");
+__device__ __forceinline__ void phase_c_append(const MatchArgs &a, int np, const bool (&keep)[kCU],
+                                               const bool (&upd)[kCU], const bool (&scan)[kCU], const int (&x)[kCU],
+                                               const int (&xs)[kCU], const int (&deg)[kCU],
+                                               unsigned long long *sh_cw, int *sh_cc, unsigned long long *sh_cb) {
+  constexpr int NW = kMatchThreads / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const Slot &N = a.slot[np];
+  unsigned long long c4 = 0ull;
+  int cch = 0, nch[kCU];
 #pragma unroll
-  for (int u = 0; u < kCU; ++u) cnt += take[u];
-  int total;
-  int ex = block_exclusive_scan<kMatchThreads>(cnt, sh_scan, &total);
-  if (threadIdx.x == 0) *sh_base = total ? atomicAdd(counter, total) : 0;
-  __syncthreads();
-  const int base = *sh_base + ex;
-  int o = 0;
+  for (int u = 0; u < kCU; ++u) {
+    const bool sm = scan[u] && deg[u] <= kSerialDeg, bg = scan[u] && deg[u] > kSerialDeg;
+    c4 += (unsigned long long)keep[u] | ((unsigned long long)upd[u] << 16) | ((unsigned long long)sm << 32) |
+          ((unsigned long long)bg << 48);
+    nch[u] = bg ? (deg[u] + kChunk - 1) / kChunk : 0;
+    cch += nch[u];
+  }
+  unsigned long long i4 = c4;
+  int ic = cch;
 #pragma unroll
-  for (int u = 0; u < kCU; ++u)
-    if (take[u]) list[base + o++] = x[u];
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long y4 = __shfl_up_sync(0xffffffffu, i4, o);
+    const int yc = __shfl_up_sync(0xffffffffu, ic, o);
+    if (lane >= o) {
+      i4 += y4;
+      ic += yc;
+    }
+  }
+  if (lane == 31) {
+    sh_cw[warp] = i4;
+    sh_cc[warp] = ic;
+  }
   __syncthreads();
+  if (warp == 0) {
+    const unsigned long long v4 = lane < NW ? sh_cw[lane] : 0ull;
+    const int vc = lane < NW ? sh_cc[lane] : 0;
+    unsigned long long j4 = v4;
+    int jc = vc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y4 = __shfl_up_sync(0xffffffffu, j4, o);
+      const int yc = __shfl_up_sync(0xffffffffu, jc, o);
+      if (lane >= o) {
+        j4 += y4;
+        jc += yc;
+      }
+    }
+    const unsigned long long t4 = __shfl_sync(0xffffffffu, j4, 31);
+    const int tc = __shfl_sync(0xffffffffu, jc, 31);
+    if (lane < NW) {
+      sh_cw[lane] = j4 - v4;
+      sh_cc[lane] = jc - vc;
+    }
+    const int f = (int)((t4 >> (16 * (lane & 3))) & 0xffffull);
+    unsigned long long gb = 0ull;
+    if (lane == 0 && f) gb = (unsigned long long)atomicAdd(a.nact + np, f);
+    if (lane == 1 && f) gb = (unsigned long long)atomicAdd(a.nupd + np, f);
+    if (lane == 2 && f) gb = (unsigned long long)atomicAdd(a.nsmall + np, f);
+    if (lane == 3 && (f || tc)) gb = atomicAdd(a.big + np, ((unsigned long long)f << 32) | (unsigned)tc);
+    if (lane < 4) sh_cb[lane] = gb;
+  }
+  __syncthreads();
+  const unsigned long long e4 = sh_cw[warp] + (i4 - c4);
+  int pk = (int)sh_cb[0] + (int)(e4 & 0xffffull);
+  int pu = (int)sh_cb[1] + (int)((e4 >> 16) & 0xffffull);
+  int ps = (int)sh_cb[2] + (int)((e4 >> 32) & 0xffffull);
+  int pb = (int)(sh_cb[3] >> 32) + (int)(e4 >> 48);
+  int pc = (int)(sh_cb[3] & 0xffffffffull) + sh_cc[warp] + (ic - cch);
+#pragma unroll
+  for (int u = 0; u < kCU; ++u) {
+    if (keep[u]) N.act[pk++] = x[u];
+    if (upd[u]) N.upd[pu++] = x[u];
+    if (scan[u] && deg[u] <= kSerialDeg) N.small[ps++] = x[u];
+    const int idx = pb, cb = pc;
+    if (nch[u] > 0) {
+      ++pb;
+      pc += nch[u];
+      N.big_v[idx] = x[u];
+      N.big_base[idx] = cb;
+      N.big_done[idx] = 0;
+    }
+    write_descs(N.desc, nch[u] > 0, x[u], xs[u], deg[u], nch[u], idx, cb);
+  }
+  __syncthreads();  // the shared counts are free for the next call
 }
 
 // Phase A of a round: full scans of the rows whose candidates must be
@@ -359,24 +606,29 @@ __device__ __forceinline__ void block_append(int *list, int *counter, const bool
 // `skip_gather`: first round with every edge eligible (no neighbour state).
 template <bool H>
 __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool first, bool skip_gather,
-                                        long long nsmall, int nchunks, int gwarp, int nwarps, int lane) {
+                                        long long nsmall, int nchunks, int gwarp, int nwarps, int lane, int2 *wbuf) {
   for (long long b0 = (long long)gwarp * 32; b0 < nsmall; b0 += (long long)nwarps * 32) {
     const long long i = b0 + lane;
     if (i >= nsmall) continue;
     const int v = first ? (int)i : __ldcg(S.small + i);
     const int xs = a.xadj[v], deg = a.xadj[v + 1] - xs;
     if (first && (deg == 0 || deg > kSerialDeg)) continue;
-    if (skip_gather) {  // first round, every edge eligible: ids and weights only
-      int k[kSerialDeg], w[kSerialDeg];
-#pragma unroll
-      for (int t = 0; t < kSerialDeg; ++t) {
-        k[t] = t < deg ? a.adjncy[xs + t] : -1;
-        w[t] = t < deg ? a.adjwgt[xs + t] : 0;
-      }
+    if (skip_gather) {  // first round, every edge eligible: ids and weights only, 8 at a time
+      constexpr int kHalf = kSerialDeg / 2;
+      const int hb = hash_base(a, v);
       TopK<H, kFirstKeepShort> tk;
+#pragma unroll 1
+      for (int t0 = 0; t0 < deg; t0 += kHalf) {
+        int k[kHalf], w[kHalf];
 #pragma unroll
-      for (int t = 0; t < kSerialDeg; ++t)
-        if (k[t] >= 0 && k[t] != v) tk.insert_edge(v, k[t], w[t], hash_base(a, v));
+        for (int t = 0; t < kHalf; ++t) {
+          k[t] = t0 + t < deg ? a.adjncy[xs + t0 + t] : -1;
+          w[t] = t0 + t < deg ? a.adjwgt[xs + t0 + t] : 0;
+        }
+#pragma unroll
+        for (int t = 0; t < kHalf; ++t)
+          if (k[t] >= 0 && k[t] != v) tk.insert_edge(v, k[t], w[t], hb);
+      }
       store_top(a, v, tk);
       continue;
     }
@@ -412,7 +664,7 @@ __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool 
       const int4 dn = q + nwarps < nchunks ? __ldcg(S.desc + q + nwarps) : d;
       const int v = d.x, i = d.w;
       constexpr int KC = kFirstKeepChunk;
-      const TopK<H, KC> r1 = warp_topk(lane_scan<H, KC>(a, v, 0, d.y, d.z, true));
+      const TopK<H, KC> r1 = chunk_best<H, KC>(a, v, 0, d.y, d.z, true, wbuf);
       if (i < 0) {
         if (lane == 0) store_top(a, v, r1);
       } else {
@@ -433,29 +685,34 @@ __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool 
         if (last) {
           __threadfence();
           const int base = __ldcg(S.big_base + i);
-          TopK<H, KC> acc;
-          for (int t = lane; t < nch * KC; t += 32)
-            acc.insert(Cand<H>::load(a.part + ((size_t)(base + t / KC) * kTop + t % KC) * kPartInts));
-          const TopK<H, KC> rr = warp_topk(acc);
+          const TopK<H, KC> rr =
+              merge_parts<H, KC>(a, nch * KC, [&](int t) { return (size_t)(base + t / KC) * kTop + t % KC; });
           if (lane == 0) store_top(a, v, rr);
         }
       }
       d = dn;
     }
   }
-  for (int q = skip_gather ? nchunks : gwarp; q < nchunks; q += nwarps) {
-    const int4 d = __ldcg(S.desc + q);
+  // Scans with the neighbours' state.  A vertex of a scan list is unmatched
+  // (the lists are built after the previous round's commits), so its row's
+  // loads are issued together with its own state; the next descriptor is
+  // loaded ahead.
+  const int q0 = skip_gather ? nchunks : gwarp;
+  int4 dcur = q0 < nchunks ? __ldcg(S.desc + q0) : make_int4(0, 0, 0, 0);
+  for (int q = q0; q < nchunks; q += nwarps) {
+    const int4 d = dcur;
+    if (q + nwarps < nchunks) dcur = __ldcg(S.desc + q + nwarps);
     const int v = d.x, i = d.w;
     const int sv = __ldcg(a.m2 + v);
-    if (sv >= 0) continue;  // uniform per warp
     const long long vw = -1ll - sv;
     TopK<H, kTop> r;
     if (first) {
-      const TopK<H, 1> r1 = warp_topk(lane_scan<H, 1>(a, v, vw, d.y, d.z, skip_gather));
+      const TopK<H, 1> r1 = chunk_best<H, 1>(a, v, vw, d.y, d.z, skip_gather, wbuf);
       r.c[0] = r1.c[0];
     } else {
-      r = warp_topk(lane_scan<H, kTop>(a, v, vw, d.y, d.z));
+      r = chunk_best<H, kTop>(a, v, vw, d.y, d.z, false, wbuf);
     }
+    if (sv >= 0) continue;  // (not expected) uniform per warp, and alike for all chunks of the row
     if (i < 0) {  // the row's only chunk
       if (lane == 0) {
         if (first) {
@@ -485,10 +742,7 @@ __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool 
     if (last) {  // merge the row's chunk lists
       __threadfence();
       const int base = __ldcg(S.big_base + i);
-      TopK<H, kTop> acc;
-      for (int t = lane; t < nch * kTop; t += 32)
-        acc.insert(Cand<H>::load(a.part + ((size_t)base * kTop + t) * kPartInts));
-      const TopK<H, kTop> rr = warp_topk(acc);
+      const TopK<H, kTop> rr = merge_parts<H, kTop>(a, nch * kTop, [&](int t) { return (size_t)base * kTop + t; });
       if (lane == 0) {
         if (first) {
           TopK<H, 1> r1;
@@ -541,21 +795,28 @@ __global__ void __launch_bounds__(kPrepThreads) k_match_prep(MatchArgs a) {
 // than the persistent kernel can hold.  When even the two heaviest vertices
 // may pair and are light (2 vmax <= maxvwgt, 3 vmax < maxvwgt), every edge is
 // eligible while nothing is matched, and the scans skip the neighbour state.
-template <bool H>
+// Both forms are launched (the choice is made on the device, from vmax); the
+// one that does not apply returns at once.  Separate kernels keep each form's
+// register allocation to its own needs.
+template <bool H, bool ALL>
 __global__ void __launch_bounds__(kPrepThreads, kFirstMinBlocks) k_match_first(MatchArgs a) {
+  const long long vmax = __ldcg(a.vmax);
+  const bool all_elig = 2 * vmax <= a.maxvwgt && 3 * vmax < a.maxvwgt;
+  if (all_elig != ALL) return;
   const int lane = threadIdx.x & 31;
   const int gwarp = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
-  const long long vmax = __ldcg(a.vmax);
-  const bool all_elig = 2 * vmax <= a.maxvwgt && 3 * vmax < a.maxvwgt;
   const int nchunks = (int)(__ldcg(a.big) & 0xffffffffu);
-  phase_a<H>(a, a.slot[0], true, all_elig, a.n, nchunks, gwarp, nwarps, lane);
+  __shared__ int2 sh_q[kPrepThreads / 32][32];
+  phase_a<H>(a, a.slot[0], true, ALL, a.n, nchunks, gwarp, nwarps, lane, sh_q[threadIdx.x >> 5]);
 }
 
 template <bool H>
 __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchArgs a) {
-  __shared__ int sh_scan[kMatchThreads / 32 + 1];
-  __shared__ int sh_base;
+  __shared__ int2 sh_q[kMatchThreads / 32][32];  // per warp: packed candidates of a chunk scan
+  __shared__ unsigned long long sh_cw[kMatchThreads / 32];  // phase C appends: per-warp packed counts
+  __shared__ int sh_cc[kMatchThreads / 32];                 // ... and chunk counts
+  __shared__ unsigned long long sh_cb[4];                   // ... and the lists' bases
   const int lane = threadIdx.x & 31;
   const long long gthread = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nthreads = (long long)gridDim.x * blockDim.x;
@@ -579,7 +840,6 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
   for (;; ++round) {
     const int par = round & 1;
     const Slot &S = a.slot[par];
-    const Slot &N = a.slot[par ^ 1];
     // round 0: the short-row scan list and the active list are the vertex range
     const long long nsmall = round == 0 ? n : __ldcg(a.nsmall + par);
     const int nupd = __ldcg(a.nupd + par);
@@ -624,7 +884,7 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
     const bool first = round == 0;
 
     // ---- phase A: full scans (the first round's ran in k_match_first) ---------
-    if (!first) phase_a<H>(a, S, false, false, nsmall, nchunks, gw, nw, lane);
+    if (!first) phase_a<H>(a, S, false, false, nsmall, nchunks, gw, nw, lane, sh_q[threadIdx.x >> 5]);
     if (!barrier()) return;
     trace(round + 1, 1, global_timer_ns());
 
@@ -712,14 +972,7 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
         }
         if (upd[u] || scan[u]) atomicMax(a.stamp + xv, round + 1);
       }
-      bool small[kCU];
-#pragma unroll
-      for (int u = 0; u < kCU; ++u) small[u] = scan[u] && deg[u] <= kSerialDeg;
-      block_append(N.act, a.nact + (par ^ 1), keep, x, sh_scan, &sh_base);
-      block_append(N.upd, a.nupd + (par ^ 1), upd, x, sh_scan, &sh_base);
-      block_append(N.small, a.nsmall + (par ^ 1), small, x, sh_scan, &sh_base);
-#pragma unroll
-      for (int u = 0; u < kCU; ++u) append_scan(a, par ^ 1, scan[u] && !small[u], x[u], xs[u], deg[u]);
+      phase_c_append(a, par ^ 1, keep, upd, scan, x, xs, deg, sh_cw, sh_cc, sh_cb);
     }
     if (!barrier()) return;
     trace(round + 1, 3, global_timer_ns());
@@ -910,12 +1163,14 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
   const unsigned fgrid = (unsigned)std::min<int64_t>((int64_t)ctx->num_sms * 8, want * 4);
   if (mode == CM_MATCH_HEM_HASH) {
     k_match_prep<true><<<pgrid, kPrepThreads, 0, s>>>(a);
-    k_match_first<true><<<fgrid, kPrepThreads, 0, s>>>(a);
+    k_match_first<true, true><<<fgrid, kPrepThreads, 0, s>>>(a);
+    k_match_first<true, false><<<fgrid, kPrepThreads, 0, s>>>(a);
   } else {
     k_match_prep<false><<<pgrid, kPrepThreads, 0, s>>>(a);
-    k_match_first<false><<<fgrid, kPrepThreads, 0, s>>>(a);
+    k_match_first<false, true><<<fgrid, kPrepThreads, 0, s>>>(a);
+    k_match_first<false, false><<<fgrid, kPrepThreads, 0, s>>>(a);
   }
-  ctx->launches += 2;
+  ctx->launches += 3;
   cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kMatchThreads), args, 0, s);
   if (e != cudaSuccess) {
     stage_end(ctx, CM_STAGE_MATCH, s);
