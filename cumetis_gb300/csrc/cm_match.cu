@@ -100,6 +100,7 @@ struct MatchArgs {
   int *nsmall, *nupd, *nact;     // [2] each
   unsigned long long *big;       // [2] = (rows << 32 | chunks)
   int *vmax;                     // largest vertex weight (zeroed before the launch)
+  int *tick;                     // [2 slots][phase A chunks, phase C spans] work tickets
   int *part;                     // per chunk: kTop x (w, h, k)
   int max_rounds;
   DevStatus *st;
@@ -606,7 +607,8 @@ __device__ __forceinline__ void phase_c_append(const MatchArgs &a, int np, const
 // `skip_gather`: first round with every edge eligible (no neighbour state).
 template <bool H>
 __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool first, bool skip_gather,
-                                        long long nsmall, int nchunks, int gwarp, int nwarps, int lane, int2 *wbuf) {
+                                        long long nsmall, int nchunks, int gwarp, int nwarps, int lane, int2 *wbuf,
+                                        int *tick) {
   for (long long b0 = (long long)gwarp * 32; b0 < nsmall; b0 += (long long)nwarps * 32) {
     const long long i = b0 + lane;
     if (i >= nsmall) continue;
@@ -695,13 +697,8 @@ __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool 
   }
   // Scans with the neighbours' state.  A vertex of a scan list is unmatched
   // (the lists are built after the previous round's commits), so its row's
-  // loads are issued together with its own state; the next descriptor is
-  // loaded ahead.
-  const int q0 = skip_gather ? nchunks : gwarp;
-  int4 dcur = q0 < nchunks ? __ldcg(S.desc + q0) : make_int4(0, 0, 0, 0);
-  for (int q = q0; q < nchunks; q += nwarps) {
-    const int4 d = dcur;
-    if (q + nwarps < nchunks) dcur = __ldcg(S.desc + q + nwarps);
+  // loads are issued together with its own state.
+  auto scan_chunk = [&](int q, const int4 &d) {
     const int v = d.x, i = d.w;
     const int sv = __ldcg(a.m2 + v);
     const long long vw = -1ll - sv;
@@ -712,7 +709,7 @@ __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool 
     } else {
       r = chunk_best<H, kTop>(a, v, vw, d.y, d.z, false, wbuf);
     }
-    if (sv >= 0) continue;  // (not expected) uniform per warp, and alike for all chunks of the row
+    if (sv >= 0) return;  // (not expected) uniform per warp, and alike for all chunks of the row
     if (i < 0) {  // the row's only chunk
       if (lane == 0) {
         if (first) {
@@ -723,7 +720,7 @@ __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool 
           store_top(a, v, r);
         }
       }
-      continue;
+      return;
     }
     const int nch = (a.xadj[v + 1] - a.xadj[v] + kChunk - 1) / kChunk;
     int last = 0;
@@ -752,6 +749,33 @@ __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool 
           store_top(a, v, rr);
         }
       }
+    }
+  };
+  if (skip_gather) return;
+  if (tick != nullptr) {
+    // Chunks taken one at a time from a ticket (rows of very different
+    // lengths and the last chunk's merge make a fixed assignment uneven); the
+    // next ticket and its descriptor are fetched before the current chunk is
+    // scanned.
+    int q = 0;
+    if (lane == 0) q = atomicAdd(tick, 1);
+    q = __shfl_sync(0xffffffffu, q, 0);
+    int4 d = q < nchunks ? __ldcg(S.desc + q) : make_int4(0, 0, 0, 0);
+    while (q < nchunks) {
+      int qn = 0;
+      if (lane == 0) qn = atomicAdd(tick, 1);
+      qn = __shfl_sync(0xffffffffu, qn, 0);
+      const int4 dn = qn < nchunks ? __ldcg(S.desc + qn) : d;
+      scan_chunk(q, d);
+      q = qn;
+      d = dn;
+    }
+  } else {
+    int4 d = gwarp < nchunks ? __ldcg(S.desc + gwarp) : make_int4(0, 0, 0, 0);
+    for (int q = gwarp; q < nchunks; q += nwarps) {
+      const int4 dn = q + nwarps < nchunks ? __ldcg(S.desc + q + nwarps) : d;
+      scan_chunk(q, d);
+      d = dn;
     }
   }
 }
@@ -808,7 +832,7 @@ __global__ void __launch_bounds__(kPrepThreads, kFirstMinBlocks) k_match_first(M
   const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
   const int nchunks = (int)(__ldcg(a.big) & 0xffffffffu);
   __shared__ int2 sh_q[kPrepThreads / 32][32];
-  phase_a<H>(a, a.slot[0], true, ALL, a.n, nchunks, gwarp, nwarps, lane, sh_q[threadIdx.x >> 5]);
+  phase_a<H>(a, a.slot[0], true, ALL, a.n, nchunks, gwarp, nwarps, lane, sh_q[threadIdx.x >> 5], nullptr);
 }
 
 template <bool H>
@@ -817,6 +841,7 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
   __shared__ unsigned long long sh_cw[kMatchThreads / 32];  // phase C appends: per-warp packed counts
   __shared__ int sh_cc[kMatchThreads / 32];                 // ... and chunk counts
   __shared__ unsigned long long sh_cb[4];                   // ... and the lists' bases
+  __shared__ int sh_tk;                                     // phase C: the block's ticket
   const int lane = threadIdx.x & 31;
   const long long gthread = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nthreads = (long long)gridDim.x * blockDim.x;
@@ -855,8 +880,6 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
     const long long nth = tail ? (long long)blockDim.x : nthreads;
     const int gw = tail ? (int)(threadIdx.x >> 5) : gwarp;
     const int nw = tail ? (int)(blockDim.x >> 5) : nwarps;
-    const int bid = tail ? 0 : (int)blockIdx.x;
-    const int nblk = tail ? 1 : (int)gridDim.x;
     auto barrier = [&]() -> bool {
       if (!tail) return grid_barrier(st, gridDim.x);
       __syncthreads();
@@ -873,18 +896,20 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
       if (gth == 0) record_error(st, CM_ERR_LIMIT, ERR_SITE_ROUNDS);
       break;
     }
-    if (gth == 0) {  // the next round's lists start empty
+    if (gth == 0) {  // the next round's lists and tickets start empty
       a.nsmall[par ^ 1] = 0;
       a.nupd[par ^ 1] = 0;
       a.nact[par ^ 1] = 0;
       a.big[par ^ 1] = 0;
+      a.tick[2 * (par ^ 1)] = 0;
+      a.tick[2 * (par ^ 1) + 1] = 0;
     }
     // A vertex's first scan keeps only its best candidate (most vertices never
     // need more); a rescan fills the whole cache.
     const bool first = round == 0;
 
     // ---- phase A: full scans (the first round's ran in k_match_first) ---------
-    if (!first) phase_a<H>(a, S, false, false, nsmall, nchunks, gw, nw, lane, sh_q[threadIdx.x >> 5]);
+    if (!first) phase_a<H>(a, S, false, false, nsmall, nchunks, gw, nw, lane, sh_q[threadIdx.x >> 5], a.tick + 2 * par);
     if (!barrier()) return;
     trace(round + 1, 1, global_timer_ns());
 
@@ -916,8 +941,16 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
 
     // ---- phase C: filter the active list, refresh stale pointers -------------
     // Blocks take kMatchThreads * kCU consecutive entries (block-wide appends).
+    // Blocks take kMatchThreads * kCU consecutive entries at a time from a
+    // ticket (a fixed assignment leaves most blocks idle once the list spans
+    // only one or two spans per block).
     const long long span = (long long)kMatchThreads * kCU;
-    for (long long b0 = (long long)bid * span; b0 < nact; b0 += (long long)nblk * span) {
+    for (;;) {
+      if (threadIdx.x == 0) sh_tk = atomicAdd(a.tick + 2 * par + 1, 1);
+      __syncthreads();
+      const long long b0 = (long long)sh_tk * span;
+      __syncthreads();
+      if (b0 >= nact) break;
       int x[kCU], p[kCU], sx[kCU], sp[kCU];
 #pragma unroll
       for (int u = 0; u < kCU; ++u) {
@@ -1140,6 +1173,7 @@ int launch_match(cm_ctx *ctx, const cm_graph *g, int32_t maxvwgt, int32_t mode, 
   a.nact = ctrs + 32;
   a.big = (unsigned long long *)(ctrs + 48);
   a.vmax = ctrs + 64;
+  a.tick = ctrs + 72;
   cudaMemsetAsync(ctrs, 0, 320, s);
   a.max_rounds = n + 8;
   a.st = ctx->d_status;
