@@ -75,46 +75,58 @@ k_cmap(int n, const int *__restrict__ xadj, const int *__restrict__ vwgt, const 
 #pragma unroll
   for (int it = 0; it < kCmapSteps; ++it) {
     const long long v = wbase + it * 32 + lane;
-    if (v >= n) continue;
-    int u = match[v];
-    if (u < 0 || u >= n) u = (int)v;
-    const unsigned long long P = tbase + pre[it];
-    if (v <= u) {
-      const int c = (int)(P >> 31);
-      const int e = (int)(P & kMask31);
-      const int xv = xadj[v], dv = xadj[v + 1] - xv;
-      const int xu = u != v ? xadj[u] : 0;
-      const int L = dv + (u != v ? xadj[u + 1] - xu : 0);
-      cmap[v] = c;
-      leader[c] = (int)v;
-      // contraction row metadata: leader's row start and length, follower's row start
-      if (row_meta) row_meta[c] = make_int4(xv, dv, xu, L);
-      cvwgt[c] = (int)((unsigned)vwgt[v] + (u != v ? (unsigned)vwgt[u] : 0u));
-      eoff[c] = e;
-      if (L > long_thr) {
-        if (L > long_chunk) {  // sorted in chunks and merged
-          const int nch = (L + long_chunk - 1) / long_chunk;
-          unsigned long long old = atomicAdd(long_ctr, (1ull << 32) | (unsigned long long)nch);
-          const int idx = (int)(old >> 32);
-          const int cbase = (int)(old & 0xffffffffu);
-          long_list[2 * idx] = c;
-          long_list[2 * idx + 1] = cbase;  // first chunk index of this row
-          for (int j = 0; j < nch; ++j) chunk_row[cbase + j] = idx;
-        } else {  // sorted whole by one block of the row's size class
-          const int cls = min(kRowClasses - 1, 31 - __clz((L - 1) / long_thr));
-          const int idx = atomicAdd(class_ctr + cls, 1);
-          class_list[class_offset(m_fine, long_thr, cls) + idx] = c;
+    int kind = -1, crow = 0;  // a leader's size class (its row goes to that class's list), and its coarse id
+    if (v < n) {
+      int u = match[v];
+      if (u < 0 || u >= n) u = (int)v;
+      const unsigned long long P = tbase + pre[it];
+      if (v <= u) {
+        const int c = (int)(P >> 31);
+        const int e = (int)(P & kMask31);
+        const int xv = xadj[v], dv = xadj[v + 1] - xv;
+        const int xu = u != v ? xadj[u] : 0;
+        const int L = dv + (u != v ? xadj[u + 1] - xu : 0);
+        cmap[v] = c;
+        leader[c] = (int)v;
+        // contraction row metadata: leader's row start and length, follower's row start
+        if (row_meta) row_meta[c] = make_int4(xv, dv, xu, L);
+        cvwgt[c] = (int)((unsigned)vwgt[v] + (u != v ? (unsigned)vwgt[u] : 0u));
+        eoff[c] = e;
+        if (L > long_thr) {
+          if (L > long_chunk) {  // sorted in chunks and merged
+            const int nch = (L + long_chunk - 1) / long_chunk;
+            unsigned long long old = atomicAdd(long_ctr, (1ull << 32) | (unsigned long long)nch);
+            const int idx = (int)(old >> 32);
+            const int cbase = (int)(old & 0xffffffffu);
+            long_list[2 * idx] = c;
+            long_list[2 * idx + 1] = cbase;  // first chunk index of this row
+            for (int j = 0; j < nch; ++j) chunk_row[cbase + j] = idx;
+          } else {  // sorted whole by one block of the row's size class
+            kind = min(kRowClasses - 1, 31 - __clz((L - 1) / long_thr));
+            crow = c;
+          }
         }
+        row_max = L > row_max ? L : row_max;
       }
-      row_max = L > row_max ? L : row_max;
+      if (v == n - 1) {  // the last vertex closes the scan
+        const unsigned long long inc =
+            P + ((v <= u) ? ((1ull << 31) |
+                             (unsigned long long)((xadj[v + 1] - xadj[v]) + (u != v ? xadj[u + 1] - xadj[u] : 0)))
+                          : 0ull);
+        const int cn = (int)(inc >> 31);
+        *d_cnvtxs = cn;
+        eoff[cn] = (int)(inc & kMask31);
+      }
     }
-    if (v == n - 1) {  // the last vertex closes the scan
-      const unsigned long long inc = P + ((v <= u) ? ((1ull << 31) | (unsigned long long)((xadj[v + 1] - xadj[v]) +
-                                                                                      (u != v ? xadj[u + 1] - xadj[u] : 0)))
-                                                   : 0ull);
-      const int cn = (int)(inc >> 31);
-      *d_cnvtxs = cn;
-      eoff[cn] = (int)(inc & kMask31);
+    // class-list appends aggregated over the lanes of equal class: one
+    // atomicAdd per class present in the warp
+    const unsigned peers = __match_any_sync(0xffffffffu, kind);
+    if (kind >= 0) {
+      const int first = __ffs(peers) - 1;
+      int base = 0;
+      if (lane == first) base = atomicAdd(class_ctr + kind, __popc(peers));
+      base = __shfl_sync(peers, base, first);
+      class_list[class_offset(m_fine, long_thr, kind) + base + __popc(peers & ((1u << lane) - 1u))] = crow;
     }
   }
 #pragma unroll

@@ -78,7 +78,7 @@ constexpr int class_cap_entries(int k) { return kTinyMax << (k + 1); }
 constexpr int class_threads(int k) {
   return class_cap_entries(k) / kClassItems < 32 ? 32 : class_cap_entries(k) / kClassItems;
 }
-// Rows above kCopySplit expanded entries are copied one block per row, the
+// Rows above kCopySplit expanded entries are copied one warp per row, the
 // others 32 rows per warp.
 constexpr int kCopySplit = 256;
 constexpr int class_items(int k) { return class_cap_entries(k) / class_threads(k); }
@@ -791,36 +791,40 @@ k_long_dedup(const int *__restrict__ long_list, const int *__restrict__ chunk_ro
 }
 
 // Moves the class rows above kCopySplit expanded entries from the stage to
-// their final place: one block per row, kCopyBatch loads in flight per
-// thread.
+// their final place: one warp per row, 2 kCopyBatch loads in flight per
+// lane.
 __global__ void __launch_bounds__(256)
 k_copy_class_rows(const int *__restrict__ class_list, const int *__restrict__ class_ctr, long long m,
                   const int *__restrict__ eoff, const int *__restrict__ ucount, const int *__restrict__ cxadj,
                   const int2 *__restrict__ stage, int *__restrict__ cadjncy, int *__restrict__ cadjwgt) {
   constexpr int k0 = ilog2(kCopySplit / kTinyMax);  // first class copied here
+  constexpr int kBatch = 2 * kCopyBatch;             // stage loads in flight per lane
+  const int lane = threadIdx.x & 31;
   int cnt[kClasses], total = 0;
 #pragma unroll
   for (int k = 0; k < kClasses; ++k) {
     cnt[k] = k >= k0 ? class_ctr[k] : 0;
     total += cnt[k];
   }
-  for (int i = blockIdx.x; i < total; i += gridDim.x) {
+  // one warp per row: many rows' metadata loads in flight per SM
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < total; i += nw) {
     int k = 0, j = i;
     while (j >= cnt[k]) j -= cnt[k++];
     const int c = class_list[class_offset(m, kTinyMax, k) + j];
     const int n = ucount[c];
     const int2 *src = stage + eoff[c];
     const long long dst = cxadj[c];
-    for (int t0 = threadIdx.x; t0 < n; t0 += kCopyBatch * 256) {
-      int2 e[kCopyBatch];
+    for (int t0 = lane; t0 < n; t0 += kBatch * 32) {
+      int2 e[kBatch];
 #pragma unroll
-      for (int u = 0; u < kCopyBatch; ++u) {
-        const int t = t0 + u * 256;
+      for (int u = 0; u < kBatch; ++u) {
+        const int t = t0 + u * 32;
         e[u] = t < n ? __ldcs(src + t) : make_int2(0, 0);
       }
 #pragma unroll
-      for (int u = 0; u < kCopyBatch; ++u) {
-        const int t = t0 + u * 256;
+      for (int u = 0; u < kBatch; ++u) {
+        const int t = t0 + u * 32;
         if (t < n) {
           cadjncy[dst + t] = e[u].x;
           cadjwgt[dst + t] = e[u].y;

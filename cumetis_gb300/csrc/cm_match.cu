@@ -658,42 +658,68 @@ __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool 
       store_top(a, v, tk);
     }
   }
+  // Chunk loop driver: chunks taken from a ticket when one is given (rows of
+  // very different lengths and the last chunk's merge make a fixed
+  // assignment uneven; the next ticket and its descriptor are fetched before
+  // the current chunk is scanned), else round robin over the warps.
+  auto drive = [&](auto &&scan) {
+    if (tick != nullptr) {
+      int q = 0;
+      if (lane == 0) q = atomicAdd(tick, 1);
+      q = __shfl_sync(0xffffffffu, q, 0);
+      int4 d = q < nchunks ? __ldcg(S.desc + q) : make_int4(0, 0, 0, 0);
+      while (q < nchunks) {
+        int qn = 0;
+        if (lane == 0) qn = atomicAdd(tick, 1);
+        qn = __shfl_sync(0xffffffffu, qn, 0);
+        const int4 dn = qn < nchunks ? __ldcg(S.desc + qn) : d;
+        scan(q, d);
+        q = qn;
+        d = dn;
+      }
+    } else {
+      int4 d = gwarp < nchunks ? __ldcg(S.desc + gwarp) : make_int4(0, 0, 0, 0);
+      for (int q = gwarp; q < nchunks; q += nwarps) {
+        const int4 dn = q + nwarps < nchunks ? __ldcg(S.desc + q + nwarps) : d;
+        scan(q, d);
+        d = dn;
+      }
+    }
+  };
   if (skip_gather) {
-    // First round, every edge eligible: no neighbour state, the next chunk's
-    // descriptor loaded ahead, multi-chunk rows merge one partial per chunk.
-    int4 d = gwarp < nchunks ? __ldcg(S.desc + gwarp) : make_int4(0, 0, 0, 0);
-    for (int q = gwarp; q < nchunks; q += nwarps) {
-      const int4 dn = q + nwarps < nchunks ? __ldcg(S.desc + q + nwarps) : d;
+    // First round, every edge eligible: no neighbour state; multi-chunk rows
+    // merge one partial per chunk.
+    drive([&](int q, const int4 &d) {
       const int v = d.x, i = d.w;
       constexpr int KC = kFirstKeepChunk;
       const TopK<H, KC> r1 = chunk_best<H, KC>(a, v, 0, d.y, d.z, true, wbuf);
       if (i < 0) {
         if (lane == 0) store_top(a, v, r1);
-      } else {
-        const int nch = (a.xadj[v + 1] - a.xadj[v] + kChunk - 1) / kChunk;
-        int last = 0;
-        if (lane < KC) {
-          Cand<H> mine = r1.c[0];
-#pragma unroll
-          for (int t = 1; t < KC; ++t)
-            if (lane == t) mine = r1.c[t];
-          mine.store(a.part + ((size_t)q * kTop + lane) * kPartInts);
-        }
-        if (lane == 0) {
-          __threadfence();
-          last = atomicAdd(S.big_done + i, 1) == nch - 1;
-        }
-        last = __shfl_sync(0xffffffffu, last, 0);
-        if (last) {
-          __threadfence();
-          const int base = __ldcg(S.big_base + i);
-          const TopK<H, KC> rr =
-              merge_parts<H, KC>(a, nch * KC, [&](int t) { return (size_t)(base + t / KC) * kTop + t % KC; });
-          if (lane == 0) store_top(a, v, rr);
-        }
+        return;
       }
-      d = dn;
-    }
+      const int nch = (a.xadj[v + 1] - a.xadj[v] + kChunk - 1) / kChunk;
+      int last = 0;
+      if (lane < KC) {
+        Cand<H> mine = r1.c[0];
+#pragma unroll
+        for (int t = 1; t < KC; ++t)
+          if (lane == t) mine = r1.c[t];
+        mine.store(a.part + ((size_t)q * kTop + lane) * kPartInts);
+      }
+      if (lane == 0) {
+        __threadfence();
+        last = atomicAdd(S.big_done + i, 1) == nch - 1;
+      }
+      last = __shfl_sync(0xffffffffu, last, 0);
+      if (last) {
+        __threadfence();
+        const int base = __ldcg(S.big_base + i);
+        const TopK<H, KC> rr =
+            merge_parts<H, KC>(a, nch * KC, [&](int t) { return (size_t)(base + t / KC) * kTop + t % KC; });
+        if (lane == 0) store_top(a, v, rr);
+      }
+    });
+    return;
   }
   // Scans with the neighbours' state.  A vertex of a scan list is unmatched
   // (the lists are built after the previous round's commits), so its row's
@@ -751,33 +777,7 @@ __device__ __forceinline__ void phase_a(const MatchArgs &a, const Slot &S, bool 
       }
     }
   };
-  if (skip_gather) return;
-  if (tick != nullptr) {
-    // Chunks taken one at a time from a ticket (rows of very different
-    // lengths and the last chunk's merge make a fixed assignment uneven); the
-    // next ticket and its descriptor are fetched before the current chunk is
-    // scanned.
-    int q = 0;
-    if (lane == 0) q = atomicAdd(tick, 1);
-    q = __shfl_sync(0xffffffffu, q, 0);
-    int4 d = q < nchunks ? __ldcg(S.desc + q) : make_int4(0, 0, 0, 0);
-    while (q < nchunks) {
-      int qn = 0;
-      if (lane == 0) qn = atomicAdd(tick, 1);
-      qn = __shfl_sync(0xffffffffu, qn, 0);
-      const int4 dn = qn < nchunks ? __ldcg(S.desc + qn) : d;
-      scan_chunk(q, d);
-      q = qn;
-      d = dn;
-    }
-  } else {
-    int4 d = gwarp < nchunks ? __ldcg(S.desc + gwarp) : make_int4(0, 0, 0, 0);
-    for (int q = gwarp; q < nchunks; q += nwarps) {
-      const int4 dn = q + nwarps < nchunks ? __ldcg(S.desc + q + nwarps) : d;
-      scan_chunk(q, d);
-      d = dn;
-    }
-  }
+  drive(scan_chunk);
 }
 
 // Before the rounds: initial state of every vertex (unmatched, no
