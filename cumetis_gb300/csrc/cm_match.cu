@@ -979,7 +979,8 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
           keep[u] = true;                    // waiting on an unmatched candidate
           continue;
         }
-        const int4 c = reinterpret_cast<const int4 *>(a.top)[xv];
+        // from L2: phase A of this kernel rewrites the caches on other SMs
+        const int4 c = __ldcg(reinterpret_cast<const int4 *>(a.top) + xv);
         const int cs[kTop] = {c.x, c.y, c.z, c.w};
         int sm[kTop];
 #pragma unroll
