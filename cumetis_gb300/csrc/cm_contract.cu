@@ -41,13 +41,21 @@ namespace {
 __host__ __device__ constexpr int ilog2(int v) { return v <= 1 ? 0 : 1 + ilog2(v >> 1); }
 
 // Tiny units: rows of at most kTinyMax entries, D = kTinyDiag diagonals per
-// unit, one warp per unit (capacity 2D entries, at most D/2 non-empty rows).
+// unit, one warp per unit (fewer than D + kTinyMax entries, at most D/2
+// non-empty rows).
 #ifndef CM_TINY_MAX
 #define CM_TINY_MAX 64
 #endif
 constexpr int kTinyMax = CM_TINY_MAX;
-constexpr int kTinyDiag = 2 * kTinyMax;
-constexpr int kTinyCap = 2 * kTinyDiag;
+// Diagonals per unit (a multiple of 32).  A unit's entries stay below
+// kTinyDiag + kTinyMax (its last row may run past the unit's diagonals by at
+// most one row), which sets the capacity.
+#ifndef CM_TINY_DIAG
+#define CM_TINY_DIAG (2 * CM_TINY_MAX)
+#endif
+constexpr int kTinyDiag = CM_TINY_DIAG;
+constexpr int kTinyCap = (kTinyDiag + kTinyMax + 31) / 32 * 32;
+static_assert(kTinyDiag % 32 == 0 && kTinyDiag >= 2 * kTinyMax && kTinyCap <= 512, "CM_TINY_DIAG");
 constexpr int kTinyItems = kTinyCap / 32;
 constexpr int kTinyRowsPerLane = kTinyDiag / 32;
 constexpr int kTinyMaxNz = kTinyDiag / 2;
@@ -285,7 +293,7 @@ template <typename K>
 struct TinySmem {
   SortPair<K> work[rslots(kTinyCap)];
   SortScratch<32> sc;
-  int rstart[kTinyMaxNz], xl[kTinyMaxNz], dl[kTinyMaxNz], xf[kTinyMaxNz];
+  int4 rmeta[kTinyMaxNz];  // per non-empty row: first entry in the unit, leader row start and length, follower row start
   int rcount[kTinyMaxNz], rfirst[kTinyMaxNz], rdst[kTinyMaxNz];
   unsigned char rowid[kTinyCap];  // sorted row of every gathered entry
   unsigned char nz_row[kTinyMaxNz];
@@ -352,10 +360,7 @@ k_tiny_units(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, con
       if (len[i] > 0) {
         const int j = ex >> 16, e0 = ex & 0xffff;
         jr[i] = j;
-        S.rstart[j] = e0;
-        S.xl[j] = md[i].x;
-        S.dl[j] = md[i].y;
-        S.xf[j] = md[i].z;
+        S.rmeta[j] = make_int4(e0, md[i].x, md[i].y, md[i].z);
         S.nz_row[j] = (unsigned char)(lane * RPL + i);
         S.rcount[j] = 0;
         ex += (1 << 16) + len[i];
@@ -366,7 +371,7 @@ k_tiny_units(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, con
     __syncwarp();
 #pragma unroll
     for (int i = 0; i < RPL; ++i)
-      if (jr[i] > 0) S.rowid[S.rstart[jr[i]]] = (unsigned char)jr[i];
+      if (jr[i] > 0) S.rowid[S.rmeta[jr[i]].x] = (unsigned char)jr[i];
     __syncwarp();
     {  // every entry's row: inclusive max-scan of the first-entry marks
       unsigned v[kTinyItems], run = 0;
@@ -402,7 +407,8 @@ k_tiny_units(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, con
         if (e < ntot) {
           const int j = S.rowid[e];
           jj[q] = j;
-          src[q] = expanded_src(e - S.rstart[j], S.xl[j], S.dl[j], S.xf[j]);
+          const int4 r = S.rmeta[j];
+          src[q] = expanded_src(e - r.x, r.y, r.z, r.w);
         }
       }
 #pragma unroll
