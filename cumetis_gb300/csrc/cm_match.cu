@@ -67,8 +67,11 @@ constexpr int kTop = 4;          // cached candidates per vertex
 #ifndef CM_TAIL_ITEMS
 #define CM_TAIL_ITEMS 4096
 #endif
+#ifndef CM_TAIL_CHUNKS
+#define CM_TAIL_CHUNKS 64
+#endif
 constexpr long long kTailItems = CM_TAIL_ITEMS;
-constexpr int kTailChunks = 64;
+constexpr int kTailChunks = CM_TAIL_CHUNKS;
 constexpr int kNotScanned = -2;  // top[v*kTop] before the first scan
 constexpr int kUnknown = -3;     // cache slot not computed (the first scan keeps only the best)
 // Candidates the first-round scans keep when every edge is eligible: short
@@ -914,16 +917,13 @@ __global__ void __launch_bounds__(kMatchThreads, kMatchMinBlocks) k_match(MatchA
     trace(round + 1, 1, global_timer_ns());
 
     // ---- phase B: commit mutual pairs ----------------------------------------
-    // Candidates that changed this round: short scans, chunked scans, cache updates.
-    const long long tot_b = nsmall + nbig + nupd;
+    // Candidates that changed this round: short scans, chunked scans, cache
+    // updates (in the first round every vertex, once).
+    const long long tot_b = first ? n : nsmall + nbig + nupd;
     for (long long i = gth; i < tot_b; i += nth) {
       int v;
       if (i < nsmall) {
         v = first ? (int)i : __ldcg(S.small + i);
-        if (first) {
-          const int deg = a.xadj[v + 1] - a.xadj[v];
-          if (deg == 0 || deg > kSerialDeg) continue;
-        }
       } else if (i < nsmall + nbig) {
         v = __ldcg(S.big_v + (i - nsmall));
       } else {
