@@ -33,7 +33,7 @@ PARAMS = [
     ("CM_FIRST_KEEP_CHUNK", 2, [1, 2, 4], "cm_match.cu"),    # ... and per chunked row
     ("CM_TAIL_ITEMS", 4096, [1024, 4096, 16384], "cm_match.cu"),  # rounds this small run in one block
     ("CM_TINY_MAX", 64, [16, 32, 64], "cm_contract.cu"),    # rows sorted in one-warp batches; larger rows by size class
-    ("CM_CHUNK", 8192, [4096, 8192], "cm_contract.cu"),      # huge-row segment (chunk) size
+    ("CM_CHUNK", 16384, [8192, 16384], "cm_contract.cu"),    # huge-row segment (chunk) size
     ("CM_CHUNK_THREADS", 1024, [512, 1024], "cm_contract.cu"),  # threads sorting one chunk
     ("CM_CLASS_ITEMS", 16, [8, 16], "cm_contract.cu"),        # entries per thread of the size-class blocks
     ("CM_MERGE_THREADS", 256, [256, 512], "cm_contract.cu"),
@@ -45,7 +45,8 @@ CHECK_TESTS = "test_long_rows or test_contract_bitexact or test_coarsen_hierarch
 
 def valid(cfg):
     """The sources' static constraints on combinations."""
-    return cfg["CM_CHUNK"] // cfg["CM_TINY_MAX"] <= 256  # at most eight size classes
+    return (cfg["CM_CHUNK"] // cfg["CM_TINY_MAX"] <= 256  # at most eight size classes
+            and cfg["CM_CHUNK"] // cfg["CM_CHUNK_THREADS"] <= 16)  # at most 16 pairs per thread of a chunk sort
 
 
 def defines_by_source(cfg):

@@ -63,7 +63,7 @@ constexpr int kTinyRowBits = ilog2(kTinyMaxNz - 1) + 1;
 static_assert(kTinyMax == 16 || kTinyMax == 32 || kTinyMax == 64, "CM_TINY_MAX: 16, 32 or 64");
 // Rows longer than kChunk are sorted in kChunk-entry chunks and merged.
 #ifndef CM_CHUNK
-#define CM_CHUNK 8192
+#define CM_CHUNK 16384
 #endif
 #ifndef CM_CHUNK_THREADS
 #define CM_CHUNK_THREADS 1024
@@ -71,7 +71,7 @@ static_assert(kTinyMax == 16 || kTinyMax == 32 || kTinyMax == 64, "CM_TINY_MAX: 
 constexpr int kChunk = CM_CHUNK;
 constexpr int kChunkThreads = CM_CHUNK_THREADS;
 constexpr int kChunkItems = kChunk / kChunkThreads;
-static_assert(kChunk == 4096 || kChunk == 8192, "CM_CHUNK: 4096 or 8192");
+static_assert(kChunk == 4096 || kChunk == 8192 || kChunk == 16384, "CM_CHUNK: 4096, 8192 or 16384");
 static_assert(kChunkItems >= 1 && kChunkItems <= 16 && kChunkItems * kChunkThreads == kChunk, "CM_CHUNK_THREADS");
 // Row classes k = 0 .. : kTinyMax * 2^k < L <= kTinyMax * 2^(k+1), up to
 // kChunk; the block of class k has max(32, cap / kClassItems) threads.
