@@ -102,7 +102,9 @@ k_cmap(int n, const int *__restrict__ xadj, const int *__restrict__ vwgt, const 
             long_list[2 * idx + 1] = cbase;  // first chunk index of this row
             for (int j = 0; j < nch; ++j) chunk_row[cbase + j] = idx;
           } else {  // sorted whole by one block of the row's size class
-            kind = min(kRowClasses - 1, 31 - __clz((L - 1) / long_thr));
+            const unsigned q = (unsigned)(L - 1) / (unsigned)(long_thr / 2);  // >= 2
+            const int b = 31 - __clz(q);
+            kind = min(kRowClasses - 1, 2 * (b - 1) + (int)((q >> (b - 1)) & 1u));
             crow = c;
           }
         }

@@ -73,23 +73,34 @@ constexpr int kChunkThreads = CM_CHUNK_THREADS;
 constexpr int kChunkItems = kChunk / kChunkThreads;
 static_assert(kChunk == 4096 || kChunk == 8192 || kChunk == 16384, "CM_CHUNK: 4096, 8192 or 16384");
 static_assert(kChunkItems >= 1 && kChunkItems <= 16 && kChunkItems * kChunkThreads == kChunk, "CM_CHUNK_THREADS");
-// Row classes k = 0 .. : kTinyMax * 2^k < L <= kTinyMax * 2^(k+1), up to
-// kChunk; the block of class k has max(32, cap / kClassItems) threads.
+// Row classes, two per octave up to kChunk (class_lo / class_hi): class 2j
+// holds the rows of kTinyMax 2^j < L <= 1.5 kTinyMax 2^j entries, class 2j+1
+// those up to kTinyMax 2^(j+1).  A class's block has max(32, cap / items)
+// threads, items = kClassItems for the power-of-two capacities and 3/4 of it
+// for the others.
 #ifndef CM_CLASS_ITEMS
 #define CM_CLASS_ITEMS 16
 #endif
 constexpr int kClassItems = CM_CLASS_ITEMS;
 static_assert(kClassItems == 4 || kClassItems == 8 || kClassItems == 16, "CM_CLASS_ITEMS: 4, 8 or 16");
-constexpr int kClasses = ilog2(kChunk / kTinyMax);
+constexpr int kClasses = 2 * ilog2(kChunk / kTinyMax);
 static_assert(kClasses <= kRowClasses, "row classes");
-constexpr int class_cap_entries(int k) { return kTinyMax << (k + 1); }
+constexpr int class_cap_entries(int k) {
+  return (k & 1) ? (kTinyMax << ((k >> 1) + 1)) : (3 * (kTinyMax << (k >> 1))) / 2;
+}
+constexpr int class_item_target(int k) { return (k & 1) ? kClassItems : (3 * kClassItems) / 4; }
 constexpr int class_threads(int k) {
-  return class_cap_entries(k) / kClassItems < 32 ? 32 : class_cap_entries(k) / kClassItems;
+  return class_cap_entries(k) / class_item_target(k) < 32 ? 32 : class_cap_entries(k) / class_item_target(k);
 }
 // Rows above kCopySplit expanded entries are copied one warp per row, the
 // others 32 rows per warp.
 constexpr int kCopySplit = 256;
 constexpr int class_items(int k) { return class_cap_entries(k) / class_threads(k); }
+constexpr bool class_shapes_exact(int k) {
+  return k >= kClasses || (class_items(k) * class_threads(k) == class_cap_entries(k) && class_items(k) <= 16 &&
+                           class_threads(k) <= 1024 && class_shapes_exact(k + 1));
+}
+static_assert(class_shapes_exact(0), "size-class block shapes");
 constexpr int kCopyBatch = 4;  // stage loads in flight per thread before their stores
 
 // Expanded entry o (0 <= o < L) of a coarse row: the leader's entries first
@@ -803,7 +814,7 @@ __global__ void __launch_bounds__(256)
 k_copy_class_rows(const int *__restrict__ class_list, const int *__restrict__ class_ctr, long long m,
                   const int *__restrict__ eoff, const int *__restrict__ ucount, const int *__restrict__ cxadj,
                   const int2 *__restrict__ stage, int *__restrict__ cadjncy, int *__restrict__ cadjwgt) {
-  constexpr int k0 = ilog2(kCopySplit / kTinyMax);  // first class copied here
+  constexpr int k0 = 2 * ilog2(kCopySplit / kTinyMax);  // first class copied here (rows above kCopySplit)
   constexpr int kBatch = 2 * kCopyBatch;             // stage loads in flight per lane
   const int lane = threadIdx.x & 31;
   int cnt[kClasses], total = 0;
@@ -913,7 +924,7 @@ void launch_classes(cm_ctx *ctx, const cm_graph *fine, const int *cmap, const in
                     int64_t row_bound) {
   constexpr int NT = class_threads(K), IT = class_items(K);
   const int64_t m = fine->nedges;
-  if (row_bound > ((int64_t)kTinyMax << K)) {
+  if (row_bound > class_lo(kTinyMax, K)) {
     const unsigned grid = grid_for((int64_t)ctx->num_sms * ctx->class_blocks_per_sm[K], class_cap(m, kTinyMax, K));
     k_class_rows<NT, IT><<<grid, NT, sizeof(SegSmem<NT, IT>), ctx->aux[K % cm_ctx::kAux]>>>(
         fine->adjncy, fine->adjwgt, cmap, eoff, row_meta, class_list + class_offset(m, kTinyMax, K), class_ctr + K,
@@ -983,9 +994,10 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
   int *chunk_cnt = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
   int *chunk_np = (int *)ws_take(ctx, (size_t)nchunks_max * 4);
   int4 *row_meta = (int4 *)ws_take(ctx, (size_t)n * 16);
-  // [0] chunked rows (rows << 32 | chunks); ints 2..9 the class counters;
-  // int 12 the last tiny unit's index
-  unsigned long long *ctr = (unsigned long long *)ws_take(ctx, 64);
+  // [0] chunked rows (rows << 32 | chunks); ints 2 .. 2 + kRowClasses - 1 the
+  // class counters; int 2 + kRowClasses the last tiny unit's index
+  static_assert(2 + kRowClasses + 1 <= 32, "contraction counter block");
+  unsigned long long *ctr = (unsigned long long *)ws_take(ctx, 128);
   unsigned long long *map_lb = (unsigned long long *)ws_take(ctx, (size_t)(map_tiles + 3) * 8);
   unsigned long long *scan_lb = (unsigned long long *)ws_take(ctx, (size_t)(scan_tiles + 3) * 8);
   int2 *stage0 = (int2 *)ws_take(ctx, (size_t)m * 8 + 8);
@@ -994,9 +1006,9 @@ int launch_contract(cm_ctx *ctx, const cm_graph *fine, const int32_t *match, int
       !chunk_np || !row_meta || !ctr || !map_lb || !scan_lb || !stage0 || !stage1)
     return cm_fail(CM_ERR_NOMEM, "contract: workspace too small");
   int *class_ctr = reinterpret_cast<int *>(ctr) + 2;
-  int *unit_last = reinterpret_cast<int *>(ctr) + 12;
+  int *unit_last = reinterpret_cast<int *>(ctr) + 2 + kRowClasses;
   DevStatus *st = ctx->d_status;
-  cudaMemsetAsync(ctr, 0, 64, s);
+  cudaMemsetAsync(ctr, 0, 128, s);
   cudaMemsetAsync(&st->max_row, 0, sizeof(int), s);
   cudaMemsetAsync(map_lb, 0, (size_t)(map_tiles + 3) * 8, s);
   cudaMemsetAsync(scan_lb, 0, (size_t)(scan_tiles + 3) * 8, s);

@@ -53,7 +53,7 @@ struct cm_ctx {
   // resident blocks per SM of the contraction's tiny-unit kernel (32- and
   // 64-bit keys) and of its row-class kernels
   int unit_blocks_per_sm[2] = {1, 1};
-  int class_blocks_per_sm[8] = {1, 1, 1, 1, 1, 1, 1, 1};
+  int class_blocks_per_sm[16] = {1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
 };
 
 // One coarsening level on the device.
@@ -116,11 +116,19 @@ int take_device_error(cm_ctx *ctx, cudaStream_t s);
 int cuda_status(cudaError_t e, const char *what);
 int check_launch(cm_ctx *ctx, const char *what);
 
-// Row classes of the contraction: class k lists the coarse rows of
-// base * 2^k < L <= base * 2^(k+1) expanded entries (L <= the chunk size),
-// at class_offset(m, base, k) of one list array, at most class_cap entries.
-constexpr int kRowClasses = 8;
-__host__ __device__ inline int64_t class_cap(int64_t m, int base, int k) { return m / ((int64_t)base << k) + 2; }
+// Row classes of the contraction, two per octave: class 2j lists the coarse
+// rows of base 2^j < L <= 1.5 base 2^j expanded entries, class 2j+1 those of
+// 1.5 base 2^j < L <= base 2^(j+1) (L <= the chunk size; base a power of two
+// >= 16), at class_offset(m, base, k) of one list array, at most class_cap
+// entries.
+constexpr int kRowClasses = 16;
+__host__ __device__ inline int64_t class_lo(int base, int k) {  // rows of class k have more entries than this
+  return (k & 1) ? (3 * ((int64_t)base << (k >> 1))) / 2 : ((int64_t)base << (k >> 1));
+}
+__host__ __device__ inline int64_t class_hi(int base, int k) {  // ... and at most this many
+  return (k & 1) ? ((int64_t)base << ((k >> 1) + 1)) : (3 * ((int64_t)base << (k >> 1))) / 2;
+}
+__host__ __device__ inline int64_t class_cap(int64_t m, int base, int k) { return m / class_lo(base, k) + 2; }
 __host__ __device__ inline int64_t class_offset(int64_t m, int base, int k) {
   int64_t o = 0;
   for (int i = 0; i < k; ++i) o += class_cap(m, base, i);

@@ -161,15 +161,16 @@ def _long_row_graph(L_leader, L_follower, extra=0, seed=0):
     return O.CSR(np.cumsum(xadj), dst, w, np.ones(n))
 
 
-@pytest.mark.parametrize("lens", [(32, 32), (32, 33), (100, 28), (64, 65), (128, 128), (128, 129), (200, 300),
+@pytest.mark.parametrize("lens", [(32, 32), (32, 33), (48, 48), (48, 49), (100, 28), (64, 65), (128, 128), (128, 129),
+                                  (200, 300), (384, 384), (384, 385), (6144, 6144), (6144, 6145),
                                   (512, 512), (512, 513), (1024, 1024), (1024, 1025), (2048, 2048), (2048, 2049),
                                   (4096, 4096), (4097, 4096), (8192, 8192), (8193, 8192), (20000, 13000),
                                   (40000, 30000)])
 def test_long_rows(ctx, lens):
     """Coarse rows at every path boundary: the one-warp batches (up to 64
-    entries), every size class (powers of two up to the 16384-entry chunk),
-    the copy split at 256, one past the chunk, and far beyond it (chunk sort,
-    merge passes, dedup, copy)."""
+    entries), the size classes (two per octave: 96, 128, 192, ... up to the
+    16384-entry chunk), the copy split at 256, one past the chunk, and far
+    beyond it (chunk sort, merge passes, dedup, copy)."""
     g = _long_row_graph(*lens, extra=500, seed=sum(lens))
     match = np.arange(g.n, dtype=np.int32)
     match[0], match[1] = 1, 0
