@@ -19,11 +19,12 @@
 //   L <= kTinyMax     : tiny units, one warp each.  Unit k owns the rows
 //                       whose diagonal (rows before + tiny entries before)
 //                       lies in [kD, (k+1)D) (D = kTinyDiag), so it holds
-//                       < 2D entries of <= D/2 rows; their (row, coarse id)
-//                       keys are sorted together.
+//                       < D + kTinyMax entries of <= D/2 rows; their
+//                       (row, coarse id) keys are sorted together.
 //   kTinyMax < L <= kChunk : one block per row, sized to the row's class
-//                       (powers of two from 64 to kChunk entries; one warp up
-//                       to 512 entries), coarse-id keys only.
+//                       (two classes per octave, capacities 1.5 and 2 times
+//                       a power of two, from 96 to kChunk entries; one warp
+//                       up to 512 entries), coarse-id keys only.
 //   L > kChunk        : huge rows.  Chunks of kChunk entries are sorted,
 //                       merged pairwise (merge path, one launch per pass) and
 //                       deduplicated.
