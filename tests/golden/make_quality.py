@@ -84,7 +84,7 @@ def main():
     ap.add_argument("--cases", default=",".join(CASES))
     ap.add_argument("--jobs", type=int, default=1)
     ap.add_argument("--seeds", default=",".join(map(str, SEEDS)),
-                    help="initial-partition seeds (rmat22_k256 uses 1-4: about 2.5 h of host time per seed)")
+                    help="initial-partition seeds (rmat22_k256 uses 1-4: about 2 h of host time per seed)")
     args = ap.parse_args()
     seeds = [int(x) for x in args.seeds.split(",")]
     if O.ref() is None:
