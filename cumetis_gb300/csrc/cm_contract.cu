@@ -818,18 +818,26 @@ k_copy_class_rows(const int *__restrict__ class_list, const int *__restrict__ cl
   constexpr int k0 = 2 * ilog2(kCopySplit / kTinyMax);  // first class copied here (rows above kCopySplit)
   constexpr int kBatch = 2 * kCopyBatch;             // stage loads in flight per lane
   const int lane = threadIdx.x & 31;
-  int cnt[kClasses], total = 0;
-#pragma unroll
-  for (int k = 0; k < kClasses; ++k) {
-    cnt[k] = k >= k0 ? class_ctr[k] : 0;
-    total += cnt[k];
+  // per class: its first row in this kernel's numbering and its list's offset
+  __shared__ int s_first[kClasses + 1];
+  __shared__ long long s_off[kClasses];
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int k = 0; k < kClasses; ++k) {
+      s_first[k] = t;
+      s_off[k] = class_offset(m, kTinyMax, k);
+      t += k >= k0 ? class_ctr[k] : 0;
+    }
+    s_first[kClasses] = t;
   }
+  __syncthreads();
+  const int total = s_first[kClasses];
   // one warp per row: many rows' metadata loads in flight per SM
   const int nw = gridDim.x * (blockDim.x >> 5);
   for (int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < total; i += nw) {
-    int k = 0, j = i;
-    while (j >= cnt[k]) j -= cnt[k++];
-    const int c = class_list[class_offset(m, kTinyMax, k) + j];
+    int k = k0;
+    while (i >= s_first[k + 1]) ++k;
+    const int c = class_list[s_off[k] + (i - s_first[k])];
     const int n = ucount[c];
     const int2 *src = stage + eoff[c];
     const long long dst = cxadj[c];
