@@ -45,8 +45,9 @@ CHECK_TESTS = "test_long_rows or test_contract_bitexact or test_coarsen_hierarch
 
 def valid(cfg):
     """The sources' static constraints on combinations."""
-    return (cfg["CM_CHUNK"] // cfg["CM_TINY_MAX"] <= 256  # at most eight size classes
-            and cfg["CM_CHUNK"] // cfg["CM_CHUNK_THREADS"] <= 16)  # at most 16 pairs per thread of a chunk sort
+    return (cfg["CM_CHUNK"] // cfg["CM_TINY_MAX"] <= 256  # at most sixteen size classes
+            and cfg["CM_CHUNK"] // cfg["CM_CHUNK_THREADS"] <= 16  # at most 16 pairs per thread of a chunk sort
+            and cfg["CM_CHUNK"] // cfg["CM_CLASS_ITEMS"] <= 1024)  # the largest class's block fits 1024 threads
 
 
 def defines_by_source(cfg):
