@@ -2,11 +2,12 @@
 //
 // block_radix_sort: stable LSD radix sort of (key, value) pairs of a block,
 // 4-bit digits.  Every thread holds ITEMS consecutive pairs in registers and
-// counts its digits in private 16-bit counters in shared memory (two digits
-// per word); one raking scan over all counters (digit-major, thread-minor)
-// gives every pair its place, and the pairs are scattered to a padded
-// scratch buffer and reloaded for the next digit.  No atomics, no warp votes:
-// about twenty-five instructions per pair and digit, four block barriers.
+// counts its digits in two registers (4 bits per digit), which it writes once
+// per pass to private 16-bit counters in shared memory (two digits per word);
+// one raking scan over all counters (digit-major, thread-minor) gives every
+// pair its place, and the pairs are scattered to a padded scratch buffer and
+// reloaded for the next digit.  No atomics, no warp votes, four block
+// barriers per digit.
 //
 // block_unique_sum: merges runs of equal keys of a sorted buffer into
 // (key, sum of the values) pairs, in order.
@@ -98,20 +99,44 @@ __device__ __forceinline__ void block_radix_sort(SortPair<K> *work, SortScratch<
   for (int pass = 0; pass < passes; ++pass) {
     const int shift = pass * kDigitBits;
     const bool last = pass == passes - 1;
-#pragma unroll
-    for (int p = 0; p < 8; ++p) cmine[p * kStride] = 0u;
     unsigned lr[ITEMS];
+    // The thread's digit counts live in two registers, 4 bits per digit
+    // (digits 0..7 in clo, 8..15 in chi), and reach the shared counter words
+    // once per pass.  A count can reach 16 only when all 16 items of the
+    // thread share one digit; that carry leaves a pattern whose fields sum
+    // to 0 or 1 instead of 16, and is recognised below.
+    unsigned clo = 0u, chi = 0u;
 #pragma unroll
     for (int k = 0; k < ITEMS; ++k) {
       lr[k] = 0u;
       if (k < kmax) {
         const unsigned d = (unsigned)(it[k].k >> shift) & 15u;
-        unsigned *const w = cmine + (d & 7u) * kStride;
-        const unsigned h = (d & 8u) << 1;
-        const unsigned c = *w;
-        lr[k] = (c >> h) & 0xffffu;
-        *w = c + (1u << h);
+        const unsigned s = (d & 7u) << 2, one = 1u << s;
+        const bool up = (d & 8u) != 0u;
+        lr[k] = ((up ? chi : clo) >> s) & 15u;
+        if (up) chi += one; else clo += one;
       }
+    }
+    bool all16 = false;
+    unsigned d0 = 0u;
+    if (ITEMS == 16 && kmax == 16) {
+      d0 = (unsigned)(it[0].k >> shift) & 15u;
+      const unsigned s0 = (d0 & 7u) << 2;
+      const unsigned ov = s0 < 28u ? 1u << (s0 + 4u) : 0u;
+      const bool up = (d0 & 8u) != 0u;
+      all16 = (up ? chi : clo) == ov && (up ? clo : chi) == 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      // word p holds the counts of digits p (low half) and p + 8 (high half)
+      const unsigned x = (clo >> (4 * q)) & 0x000f000fu, y = (chi >> (4 * q)) & 0x000f000fu;
+      cmine[q * kStride] = __byte_perm(x, y, 0x5410);
+      cmine[(q + 4) * kStride] = __byte_perm(x, y, 0x7632);
+    }
+    if (all16) {
+#pragma unroll
+      for (int p = 0; p < 8; ++p) cmine[p * kStride] = 0u;
+      cmine[(d0 & 7u) * kStride] = 16u << ((d0 & 8u) << 1);
     }
     __syncthreads();
     unsigned cw[8], sum = 0u;
