@@ -17,6 +17,10 @@
 
 #include "cm_device.cuh"
 
+#ifndef CM_SORT_RERANK_NT
+#define CM_SORT_RERANK_NT 1024
+#endif
+
 namespace cm {
 
 // Padded shared-memory index for keys of type K: one spare word every 32
@@ -99,6 +103,9 @@ __device__ __forceinline__ void block_radix_sort(SortPair<K> *work, SortScratch<
   for (int pass = 0; pass < passes; ++pass) {
     const int shift = pass * kDigitBits;
     const bool last = pass == passes - 1;
+    // Blocks of CM_SORT_RERANK_NT threads or more (64 registers a thread) recount
+    // the ranks in the scatter loop instead of keeping them in registers.
+    constexpr bool kRerank = NT >= CM_SORT_RERANK_NT;
     unsigned lr[ITEMS];
     // The thread's digit counts live in two registers, 4 bits per digit
     // (digits 0..7 in clo, 8..15 in chi), and reach the shared counter words
@@ -113,7 +120,7 @@ __device__ __forceinline__ void block_radix_sort(SortPair<K> *work, SortScratch<
         const unsigned d = (unsigned)(it[k].k >> shift) & 15u;
         const unsigned s = (d & 7u) << 2, one = 1u << s;
         const bool up = (d & 8u) != 0u;
-        lr[k] = ((up ? chi : clo) >> s) & 15u;
+        if (!kRerank) lr[k] = ((up ? chi : clo) >> s) & 15u;
         if (up) chi += one; else clo += one;
       }
     }
@@ -172,12 +179,23 @@ __device__ __forceinline__ void block_radix_sort(SortPair<K> *work, SortScratch<
 #pragma unroll
     for (int j = 0; j < 8; ++j) crake[j] = base + cw[j];
     __syncthreads();
+    if (kRerank) {
+      clo = 0u;
+      chi = 0u;
+    }
 #pragma unroll
     for (int k = 0; k < ITEMS; ++k) {
       if (k < kmax) {
         const unsigned d = (unsigned)(it[k].k >> shift) & 15u;
         const unsigned c = cmine[(d & 7u) * kStride];
-        const int pos = (int)(((c >> ((d & 8u) << 1)) & 0xffffu) + lr[k]);
+        unsigned lrk = lr[k];
+        if (kRerank) {
+          const unsigned s = (d & 7u) << 2, one = 1u << s;
+          const bool up = (d & 8u) != 0u;
+          lrk = ((up ? chi : clo) >> s) & 15u;
+          if (up) chi += one; else clo += one;
+        }
+        const int pos = (int)(((c >> ((d & 8u) << 1)) & 0xffffu) + lrk);
         if (last) {
           if (pos < n) work[pos] = it[k];
         } else {
