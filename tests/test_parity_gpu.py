@@ -184,6 +184,50 @@ def test_long_rows(ctx, lens):
     assert_same_graph(got, want, str(lens))
 
 
+def _repeated_neighbour_graph(lens, pool, run, seed):
+    """Hub pairs (2i, 2i+1), i < len(lens), whose leaders hold lens[i]
+    parallel entries to `pool` leaf pairs, in runs of `run` equal neighbours
+    (run = 0: one neighbour per row); the leaves' rows hold the reverse
+    entries, so they are long runs of a few hubs.  Weights include 2^30, so
+    merged weights wrap.  Returns the graph and its matching (hubs and
+    leaves paired (2i, 2i+1))."""
+    rng = np.random.default_rng(seed)
+    nh = len(lens)
+    leaves = 2 * nh + 2 * np.arange(pool)
+    src, dst = [], []
+    for i, L in enumerate(lens):
+        if run == 0:
+            nb = np.full(L, leaves[i % pool])
+        else:
+            nb = np.repeat(rng.choice(leaves, -(-L // run)), run)[:L]
+        src.append(np.full(L, 2 * i))
+        dst.append(nb + rng.integers(0, 2, L))       # either vertex of a leaf pair
+    src, dst = np.concatenate(src), np.concatenate(dst)
+    w = rng.choice(np.array([1, 7, 1 << 30], np.int64), len(src))
+    s2, d2, w2 = np.r_[src, dst], np.r_[dst, src], np.r_[w, w]
+    order = np.argsort(s2, kind="stable")             # grouped by row, construction order within
+    s2, d2, w2 = s2[order], d2[order], w2[order]
+    n = 2 * nh + 2 * pool
+    xadj = np.zeros(n + 1, np.int64)
+    np.add.at(xadj, s2 + 1, 1)
+    match = (np.arange(n) ^ 1).astype(np.int32)
+    return O.CSR(np.cumsum(xadj), d2, w2.astype(np.int32), np.ones(n)), match
+
+
+@pytest.mark.parametrize("pool,run", [(1, 0), (3, 16), (5, 17), (40, 7)])
+def test_rows_of_repeated_neighbours(ctx, pool, run):
+    """Rows whose entries are one coarse id, or long runs of a few, filling
+    the 16-item size classes (481-512, 1000, 2000, 4000, 8000, 16000, 16384
+    entries) and the chunked path: a thread's 16 pairs then share a digit in
+    every radix pass, the one case whose digit count does not fit 4 bits."""
+    lens = [481, 512, 1000, 2000, 4000, 8000, 16000, 16384, 40000]
+    g, match = _repeated_neighbour_graph(lens, pool, run, seed=pool * 100 + run)
+    want, wcmap = O.contract(g, match)
+    got, gcmap = gpu_contract(ctx, g, match)
+    assert np.array_equal(gcmap, wcmap)
+    assert_same_graph(got, want, "pool %d run %d" % (pool, run))
+
+
 def test_many_long_rows(ctx):
     """Many hubs at once (R-MAT skew at a size the oracle finishes quickly)."""
     g = _o(cm.gen_rmat(16, 32, a=0.6, b=0.15, c=0.15, seed=5))
