@@ -172,8 +172,54 @@ __device__ __forceinline__ int segment_sorted_unique(SegSmem<NT, ITEMS> &S, int 
 
 // Rows of one size class: one block per row writes the row's unique entries
 // to stage[eoff[c] ...) and their number to ucount[c].
+// Resident blocks per SM asked of the compiler for a class shape (0: no
+// bound).  Left to itself the compiler gives these shapes 71-117 registers,
+// so that registers, not shared memory, cap their blocks per SM; the bounds
+// bring them to 56-72 registers without spills (nvcc 13.0, sm_103a), e.g.
+// <256,16> from 2 to 3 blocks and <64,16> from 10 to 14.  The shapes left at
+// 0 spill under any bound that would add a block.
+#ifndef CM_MB_32_12
+#define CM_MB_32_12 32
+#endif
+#ifndef CM_MB_32_16
+#define CM_MB_32_16 22
+#endif
+#ifndef CM_MB_64_16
+#define CM_MB_64_16 13
+#endif
+#ifndef CM_MB_128_12
+#define CM_MB_128_12 9
+#endif
+#ifndef CM_MB_128_16
+#define CM_MB_128_16 6
+#endif
+#ifndef CM_MB_256_16
+#define CM_MB_256_16 3
+#endif
+#ifndef CM_MB_64_12
+#define CM_MB_64_12 0
+#endif
+#ifndef CM_MB_256_12
+#define CM_MB_256_12 0
+#endif
+#ifndef CM_MB_512_16
+#define CM_MB_512_16 0
+#endif
 template <int NT, int ITEMS>
-__global__ void __launch_bounds__(NT)
+constexpr int class_min_blocks() {
+  return (NT == 32 && ITEMS == 12)    ? CM_MB_32_12
+         : (NT == 32 && ITEMS == 16)  ? CM_MB_32_16
+         : (NT == 64 && ITEMS == 12)  ? CM_MB_64_12
+         : (NT == 64 && ITEMS == 16)  ? CM_MB_64_16
+         : (NT == 128 && ITEMS == 12) ? CM_MB_128_12
+         : (NT == 128 && ITEMS == 16) ? CM_MB_128_16
+         : (NT == 256 && ITEMS == 12) ? CM_MB_256_12
+         : (NT == 256 && ITEMS == 16) ? CM_MB_256_16
+         : (NT == 512 && ITEMS == 16) ? CM_MB_512_16
+                                      : 0;
+}
+template <int NT, int ITEMS>
+__global__ void __launch_bounds__(NT, class_min_blocks<NT, ITEMS>())
 k_class_rows(const int *__restrict__ adjncy, const int *__restrict__ adjwgt, const int *__restrict__ cmap,
              const int *__restrict__ eoff, const int4 *__restrict__ row_meta, const int *__restrict__ list,
              const int *__restrict__ count, const int *d_cn, int2 *__restrict__ stage, int *__restrict__ ucount) {
