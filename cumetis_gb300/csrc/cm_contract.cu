@@ -176,8 +176,9 @@ __device__ __forceinline__ int segment_sorted_unique(SegSmem<NT, ITEMS> &S, int 
 // bound).  Left to itself the compiler gives these shapes 71-117 registers,
 // so that registers, not shared memory, cap their blocks per SM; the bounds
 // bring them to 56-72 registers without spills (nvcc 13.0, sm_103a), e.g.
-// <256,16> from 2 to 3 blocks and <64,16> from 10 to 14.  The shapes left at
-// 0 spill under any bound that would add a block.
+// <256,16> from 2 to 3 blocks and <64,16> from 10 to 14.  <512,16> at 2
+// blocks (64 registers, 28 bytes spilled) still gains a little; <64,12> and
+// <256,12> spill under any bound that would add a block and gain nothing.
 #ifndef CM_MB_32_12
 #define CM_MB_32_12 32
 #endif
@@ -203,7 +204,7 @@ __device__ __forceinline__ int segment_sorted_unique(SegSmem<NT, ITEMS> &S, int 
 #define CM_MB_256_12 0
 #endif
 #ifndef CM_MB_512_16
-#define CM_MB_512_16 0
+#define CM_MB_512_16 2
 #endif
 template <int NT, int ITEMS>
 constexpr int class_min_blocks() {
