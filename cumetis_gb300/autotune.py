@@ -5,7 +5,8 @@
 Each tuning parameter is a macro of one CUDA source (the warp-per-vertex
 threshold and the warp work-item size of the matching, the longest row the
 contraction sorts in one-warp batches and its chunk size, the block shapes of
-their kernels).  The search is coordinate descent from the current tuning file (or
+their kernels, the resident blocks per SM each size-class shape is compiled
+for).  The search is coordinate descent from the current tuning file (or
 the compiled-in defaults): for each parameter in turn every other candidate
 value is built as a library variant (only the source it belongs to is
 recompiled), timed with bench.py in a fresh process on the same workload,
@@ -37,6 +38,14 @@ PARAMS = [
     ("CM_CHUNK_THREADS", 1024, [512, 1024], "cm_contract.cu"),  # threads sorting one chunk
     ("CM_CLASS_ITEMS", 16, [8, 16], "cm_contract.cu"),        # entries per thread of the size-class blocks
     ("CM_MERGE_THREADS", 256, [256, 512], "cm_contract.cu"),
+    # resident blocks per SM asked of the compiler for a size-class shape (0: no launch bound)
+    ("CM_MB_32_12", 32, [0, 32], "cm_contract.cu"),
+    ("CM_MB_32_16", 22, [0, 22, 28], "cm_contract.cu"),
+    ("CM_MB_64_16", 13, [0, 13, 16], "cm_contract.cu"),
+    ("CM_MB_128_12", 9, [0, 9, 12], "cm_contract.cu"),
+    ("CM_MB_128_16", 6, [0, 6, 8], "cm_contract.cu"),
+    ("CM_MB_256_16", 3, [0, 3, 4], "cm_contract.cu"),
+    ("CM_MB_512_16", 2, [0, 2], "cm_contract.cu"),
 ]
 DEFAULTS = {name: d for name, d, _, _ in PARAMS}
 SOURCE = {name: src for name, _, _, src in PARAMS}
